@@ -1,0 +1,153 @@
+/*
+ * pcgpu.h -- C ABI of the GB300 hard-special-leaf engine (libpcgpu.so).
+ *
+ * The engine computes the hard special leaves of combinatorial prime
+ * counting on one GPU: Gourdon's D(x, y, z, k) and Deleglise-Rivat's
+ * S2_hard(x, y, z, c), and on top of them pi(x) and phi(x, a), single and
+ * batched.  Every entry point is extern "C", takes plain integers and
+ * pointers, never throws, and returns a pcg_status; the message of the last
+ * failure is available from pcg_last_error().
+ *
+ * 128-bit integers use pcg_i128, the layout of the reference's
+ * pc_int128_t (include/primecount.h:38-41): { uint64_t lo; int64_t hi; }.
+ *
+ * Reference interfaces replaced (kimwalisch/primecount 8.7):
+ *   pcg_D          <- int64_t/int128_t D(x, y, z, k, threads, is_print)
+ *                     include/gourdon.hpp:28,38; src/gourdon/D.cpp:425-505
+ *   pcg_S2_hard    <- int64_t/int128_t S2_hard(x, y, z, c, threads, is_print)
+ *                     include/S.hpp:25,32; src/deleglise-rivat/S2_hard.cpp:221-293
+ *   pcg_pi         <- primecount::pi(int64_t / pc_int128_t)
+ *                     include/primecount.hpp:57-66; src/api.cpp:44-91
+ *   pcg_phi        <- primecount::phi(x, a)  include/primecount.hpp:99; src/api.cpp:246
+ *   pcg_pi_batch, pcg_phi_batch: many queries per call (no counterpart: the
+ *                     reference answers one query per call)
+ *   pcg_ctx_*      : device-resident tables (no counterpart: the reference
+ *                     builds its tables inside every call, D.cpp:443-446)
+ *   primecount_pi / primecount_pi_128 / primecount_phi /
+ *   primecount_get_num_threads / primecount_set_num_threads /
+ *   primecount_version
+ *                  <- the libprimecount C API, include/primecount.h:51-122,
+ *                     src/api_c.cpp:19-150 (same names, same -1 error
+ *                     convention, message printed to stderr)
+ */
+#ifndef PCGPU_H
+#define PCGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+  uint64_t lo;
+  int64_t hi;
+} pcg_i128;
+
+typedef enum {
+  PCG_OK = 0,
+  PCG_EINVAL = 1,     /* invalid argument (negative x, y < 1, ...)          */
+  PCG_ERANGE = 2,     /* input beyond the supported range (x > y * 2^62, ...)*/
+  PCG_ENOMEM = 3,     /* device or host allocation failed / over budget     */
+  PCG_ECUDA = 4,      /* a CUDA call failed                                 */
+  PCG_ENODEV = 5,     /* no CUDA device                                     */
+  PCG_ETIMEOUT = 6,   /* a bounded device wait gave up                      */
+  PCG_ECANCELLED = 7, /* request cancelled (serving)                        */
+  PCG_EINTERNAL = 8   /* internal consistency check failed                  */
+} pcg_status;
+
+typedef struct pcg_ctx pcg_ctx;
+
+/* Options of one call.  A NULL pcg_opts* means all defaults. */
+typedef struct {
+  pcg_ctx* ctx;          /* NULL: the library's default context of the current device */
+  void* stream;          /* cudaStream_t to launch on; NULL: the context's stream      */
+  int threads;           /* host threads (reference `threads`); 0 = all                */
+  int print;             /* reference is_print: print variables and timings            */
+  int segment_words;     /* sieve segment in 64-bit words (x240 numbers); 0 = autotune */
+  int ctas_per_sm;       /* resident CTAs per SM for the sweep; 0 = autotune           */
+} pcg_opts;
+
+/* Work and time of the last call on a context. */
+typedef struct {
+  uint64_t leaves;         /* hard special leaves evaluated                          */
+  uint64_t two_prime_leaves;/* of which p_b * p_l leaves                              */
+  uint64_t segments;       /* sieve segments                                          */
+  uint64_t levels;         /* (segment, b) sieve steps                                */
+  uint64_t factor_entries; /* FactorTable entries read by the leaf filter             */
+  uint64_t kernel_launches;/* engine kernels launched by the call                     */
+  double table_ms;         /* device table construction (0 when resident)            */
+  double sweep_ms;         /* sieve + leaf kernels                                    */
+  double combine_ms;       /* phi-offset scan and reduction                           */
+  double total_ms;         /* whole call, host clock                                  */
+  int segment_words;       /* tuning actually used                                    */
+  int ctas_per_sm;
+  int threads_per_cta;
+} pcg_stats;
+
+/* ---- contexts: device-resident prime / PiTable / FactorTable state ---- */
+
+/* Create a context on the current CUDA device whose tables cover every
+ * query with x <= max_x (Gourdon default parameters).  mem_budget bounds
+ * the device memory the context may hold (0 = 90% of free memory). */
+pcg_status pcg_ctx_create(pcg_i128 max_x, uint64_t mem_budget, pcg_ctx** out);
+void pcg_ctx_destroy(pcg_ctx* ctx);
+/* Message of the last failure on ctx (NULL: of the calling thread). */
+const char* pcg_last_error(const pcg_ctx* ctx);
+/* Statistics of the last D / S2_hard / pi call on ctx (NULL: default ctx). */
+pcg_status pcg_last_stats(const pcg_ctx* ctx, pcg_stats* out);
+/* Device bytes held by the context's resident tables. */
+uint64_t pcg_ctx_device_bytes(const pcg_ctx* ctx);
+
+/* ---- the hard-leaf formulas ---- */
+
+/* D(x, y, z, k): Gourdon's hard special leaves. */
+pcg_status pcg_D(pcg_i128 x, int64_t y, int64_t z, int64_t k,
+                 const pcg_opts* opts, pcg_i128* out);
+
+/* S2_hard(x, y, z, c): Deleglise-Rivat's hard special leaves. */
+pcg_status pcg_S2_hard(pcg_i128 x, int64_t y, int64_t z, int64_t c,
+                       const pcg_opts* opts, pcg_i128* out);
+
+/* D(x) / S2_hard(x) with the reference's default parameters
+ * (the --D / --S2-hard command-line options, src/app/main.cpp:205-246,
+ * 435-461).  y, z, k (c) are written when the pointers are non-NULL. */
+pcg_status pcg_D_default(pcg_i128 x, const pcg_opts* opts, pcg_i128* out,
+                         int64_t* y, int64_t* z, int64_t* k);
+pcg_status pcg_S2_hard_default(pcg_i128 x, const pcg_opts* opts, pcg_i128* out,
+                               int64_t* y, int64_t* z, int64_t* c);
+
+/* Gourdon / Deleglise-Rivat parameters as the reference picks them
+ * (src/gourdon/pi_gourdon.cpp:44-62, src/util.cpp:222-386). */
+pcg_status pcg_gourdon_params(pcg_i128 x, int64_t* y, int64_t* z, int64_t* k,
+                              int64_t* x_star);
+pcg_status pcg_dr_params(pcg_i128 x, int64_t* y, int64_t* z, int64_t* c);
+
+/* ---- prime counting on top of the engine ---- */
+
+/* pi(x), x < 2^127; -1 semantics are left to the primecount_* wrappers. */
+pcg_status pcg_pi(pcg_i128 x, const pcg_opts* opts, pcg_i128* out);
+/* phi(x, a): numbers <= x not divisible by any of the first a primes. */
+pcg_status pcg_phi(int64_t x, int64_t a, const pcg_opts* opts, int64_t* out);
+
+/* n independent pi(x) queries (x may differ wildly in size). */
+pcg_status pcg_pi_batch(const pcg_i128* xs, size_t n, pcg_i128* out,
+                        const pcg_opts* opts);
+/* n independent phi(x, a) queries. */
+pcg_status pcg_phi_batch(const int64_t* x, const int64_t* a, size_t n,
+                         int64_t* out, const pcg_opts* opts);
+
+/* ---- libprimecount C API (same names and error convention) ---- */
+int64_t primecount_pi(int64_t x);
+pcg_i128 primecount_pi_128(pcg_i128 x);
+int64_t primecount_phi(int64_t x, int64_t a);
+int primecount_get_num_threads(void);
+void primecount_set_num_threads(int num_threads);
+const char* primecount_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

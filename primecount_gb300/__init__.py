@@ -1,0 +1,242 @@
+"""primecount_gb300 -- Python mirror of the GB300 hard-special-leaf engine.
+
+The compute lives in libpcgpu.so (CUDA, sm_103a) behind the C ABI of
+include/pcgpu.h; this module binds it with ctypes and mirrors the
+reference's interface (kimwalisch/primecount 8.7, include/primecount.hpp and
+the internal formula functions of include/gourdon.hpp / include/S.hpp):
+
+    pi(x), phi(x, a)                      primecount::pi / primecount::phi
+    D(x, y, z, k), S2_hard(x, y, z, c)    internal formula functions
+    D_default(x), S2_hard_default(x)      the --D / --S2-hard CLI options
+    pi_batch(xs), phi_batch(xs, as)       many queries per call (new)
+    Context(max_x)                        device-resident tables (new)
+
+Errors raise PrimecountError (the reference's primecount_error).  There is
+no CPU fallback: without the CUDA library or a GPU every call raises.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libpcgpu.so")
+
+PCG_OK = 0
+STATUS = {0: "PCG_OK", 1: "PCG_EINVAL", 2: "PCG_ERANGE", 3: "PCG_ENOMEM", 4: "PCG_ECUDA",
+          5: "PCG_ENODEV", 6: "PCG_ETIMEOUT", 7: "PCG_ECANCELLED", 8: "PCG_EINTERNAL"}
+
+
+class PrimecountError(RuntimeError):
+    """Mirror of the reference's primecount_error; .status holds the pcg_status."""
+
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (STATUS.get(status, status), msg))
+        self.status = status
+
+
+class I128(ctypes.Structure):
+    _fields_ = [("lo", ctypes.c_uint64), ("hi", ctypes.c_int64)]
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("ctx", ctypes.c_void_p), ("stream", ctypes.c_void_p), ("threads", ctypes.c_int),
+                ("print", ctypes.c_int), ("segment_words", ctypes.c_int), ("ctas_per_sm", ctypes.c_int)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("leaves", ctypes.c_uint64), ("two_prime_leaves", ctypes.c_uint64),
+                ("segments", ctypes.c_uint64), ("levels", ctypes.c_uint64),
+                ("factor_entries", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
+                ("table_ms", ctypes.c_double), ("sweep_ms", ctypes.c_double),
+                ("combine_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
+                ("segment_words", ctypes.c_int), ("ctas_per_sm", ctypes.c_int),
+                ("threads_per_cta", ctypes.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def to_i128(v):
+    v = int(v)
+    return I128(v & 0xFFFFFFFFFFFFFFFF, v >> 64)
+
+
+def from_i128(r):
+    return (int(r.hi) << 64) | int(r.lo)
+
+
+_lib = None
+
+
+def load(path=None):
+    """Load libpcgpu.so (raises PrimecountError if it was not built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise PrimecountError(5, "libpcgpu.so not built (python -m primecount_gb300.build): %s" % p)
+    L = ctypes.CDLL(p)
+    c_i64, c_p = ctypes.c_int64, ctypes.POINTER
+    L.pcg_D.argtypes = [I128, c_i64, c_i64, c_i64, c_p(Opts), c_p(I128)]
+    L.pcg_S2_hard.argtypes = [I128, c_i64, c_i64, c_i64, c_p(Opts), c_p(I128)]
+    L.pcg_D_default.argtypes = [I128, c_p(Opts), c_p(I128), c_p(c_i64), c_p(c_i64), c_p(c_i64)]
+    L.pcg_S2_hard_default.argtypes = [I128, c_p(Opts), c_p(I128), c_p(c_i64), c_p(c_i64), c_p(c_i64)]
+    L.pcg_gourdon_params.argtypes = [I128, c_p(c_i64), c_p(c_i64), c_p(c_i64), c_p(c_i64)]
+    L.pcg_dr_params.argtypes = [I128, c_p(c_i64), c_p(c_i64), c_p(c_i64)]
+    L.pcg_pi.argtypes = [I128, c_p(Opts), c_p(I128)]
+    L.pcg_phi.argtypes = [c_i64, c_i64, c_p(Opts), c_p(c_i64)]
+    L.pcg_pi_batch.argtypes = [c_p(I128), ctypes.c_size_t, c_p(I128), c_p(Opts)]
+    L.pcg_phi_batch.argtypes = [c_p(c_i64), c_p(c_i64), ctypes.c_size_t, c_p(c_i64), c_p(Opts)]
+    L.pcg_ctx_create.argtypes = [I128, ctypes.c_uint64, c_p(ctypes.c_void_p)]
+    L.pcg_ctx_destroy.argtypes = [ctypes.c_void_p]
+    L.pcg_ctx_destroy.restype = None
+    L.pcg_last_error.argtypes = [ctypes.c_void_p]
+    L.pcg_last_error.restype = ctypes.c_char_p
+    L.pcg_last_stats.argtypes = [ctypes.c_void_p, c_p(Stats)]
+    L.pcg_ctx_device_bytes.argtypes = [ctypes.c_void_p]
+    L.pcg_ctx_device_bytes.restype = ctypes.c_uint64
+    L.primecount_pi.argtypes = [c_i64]
+    L.primecount_pi.restype = c_i64
+    L.primecount_pi_128.argtypes = [I128]
+    L.primecount_pi_128.restype = I128
+    L.primecount_phi.argtypes = [c_i64, c_i64]
+    L.primecount_phi.restype = c_i64
+    L.primecount_version.restype = ctypes.c_char_p
+    for name in ("pcg_D", "pcg_S2_hard", "pcg_D_default", "pcg_S2_hard_default", "pcg_gourdon_params",
+                 "pcg_dr_params", "pcg_pi", "pcg_phi", "pcg_pi_batch", "pcg_phi_batch", "pcg_ctx_create",
+                 "pcg_last_stats"):
+        getattr(L, name).restype = ctypes.c_int
+    if path is None:
+        _lib = L
+    return L
+
+
+def _check(st, ctx=None):
+    if st != PCG_OK:
+        L = load()
+        msg = L.pcg_last_error(ctx._h if ctx is not None else None)
+        raise PrimecountError(st, (msg or b"").decode())
+
+
+class Context:
+    """Device-resident primes / PiTable / FactorTable sized for x <= max_x."""
+
+    def __init__(self, max_x=0, mem_budget=0):
+        L = load()
+        h = ctypes.c_void_p()
+        st = L.pcg_ctx_create(to_i128(max_x), int(mem_budget), ctypes.byref(h))
+        if st != PCG_OK:
+            raise PrimecountError(st, (L.pcg_last_error(None) or b"").decode())
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().pcg_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def device_bytes(self):
+        return int(load().pcg_ctx_device_bytes(self._h))
+
+    def last_stats(self):
+        s = Stats()
+        _check(load().pcg_last_stats(self._h, ctypes.byref(s)), self)
+        return s.as_dict()
+
+
+def _opts(ctx=None, stream=None, threads=0, print_=False, segment_words=0, ctas_per_sm=0):
+    o = Opts()
+    o.ctx = ctx._h if ctx is not None else None
+    o.stream = stream
+    o.threads = threads
+    o.print = 1 if print_ else 0
+    o.segment_words = segment_words
+    o.ctas_per_sm = ctas_per_sm
+    return o
+
+
+def last_stats(ctx=None):
+    s = Stats()
+    _check(load().pcg_last_stats(ctx._h if ctx is not None else None, ctypes.byref(s)), ctx)
+    return s.as_dict()
+
+
+def D(x, y, z, k, threads=0, print=False, ctx=None, stream=None, segment_words=0, ctas_per_sm=0):
+    """Gourdon's D(x, y, z, k): the hard special leaves (src/gourdon/D.cpp)."""
+    out = I128()
+    o = _opts(ctx, stream, threads, print, segment_words, ctas_per_sm)
+    _check(load().pcg_D(to_i128(x), int(y), int(z), int(k), ctypes.byref(o), ctypes.byref(out)), ctx)
+    return from_i128(out)
+
+
+def S2_hard(x, y, z, c, threads=0, print=False, ctx=None, stream=None, segment_words=0, ctas_per_sm=0):
+    """Deleglise-Rivat's S2_hard(x, y, z, c) (src/deleglise-rivat/S2_hard.cpp)."""
+    out = I128()
+    o = _opts(ctx, stream, threads, print, segment_words, ctas_per_sm)
+    _check(load().pcg_S2_hard(to_i128(x), int(y), int(z), int(c), ctypes.byref(o), ctypes.byref(out)), ctx)
+    return from_i128(out)
+
+
+def gourdon_params(x):
+    y, z, k, xs = (ctypes.c_int64() for _ in range(4))
+    _check(load().pcg_gourdon_params(to_i128(x), ctypes.byref(y), ctypes.byref(z), ctypes.byref(k),
+                                     ctypes.byref(xs)))
+    return {"y": y.value, "z": z.value, "k": k.value, "x_star": xs.value}
+
+
+def dr_params(x):
+    y, z, c = (ctypes.c_int64() for _ in range(3))
+    _check(load().pcg_dr_params(to_i128(x), ctypes.byref(y), ctypes.byref(z), ctypes.byref(c)))
+    return {"y": y.value, "z": z.value, "c": c.value}
+
+
+def D_default(x, **kw):
+    """D(x) with the reference's default y, z, k (the --D option)."""
+    p = gourdon_params(x)
+    return D(x, p["y"], p["z"], p["k"], **kw)
+
+
+def S2_hard_default(x, **kw):
+    """S2_hard(x) with the reference's default y, z, c (the --S2-hard option)."""
+    p = dr_params(x)
+    return S2_hard(x, p["y"], p["z"], p["c"], **kw)
+
+
+def pi(x, threads=0, print=False, ctx=None, stream=None):
+    """Number of primes <= x (primecount::pi)."""
+    out = I128()
+    o = _opts(ctx, stream, threads, print)
+    _check(load().pcg_pi(to_i128(x), ctypes.byref(o), ctypes.byref(out)), ctx)
+    return from_i128(out)
+
+
+def phi(x, a, threads=0, ctx=None, stream=None):
+    """Partial sieve function phi(x, a) (primecount::phi)."""
+    out = ctypes.c_int64()
+    o = _opts(ctx, stream, threads)
+    _check(load().pcg_phi(int(x), int(a), ctypes.byref(o), ctypes.byref(out)), ctx)
+    return out.value
+
+
+def pi_batch(xs, ctx=None, stream=None):
+    n = len(xs)
+    arr = (I128 * n)(*[to_i128(v) for v in xs])
+    out = (I128 * n)()
+    o = _opts(ctx, stream)
+    _check(load().pcg_pi_batch(arr, n, out, ctypes.byref(o)), ctx)
+    return [from_i128(v) for v in out]
+
+
+def phi_batch(xs, as_, ctx=None, stream=None):
+    n = len(xs)
+    ax = (ctypes.c_int64 * n)(*[int(v) for v in xs])
+    aa = (ctypes.c_int64 * n)(*[int(v) for v in as_])
+    out = (ctypes.c_int64 * n)()
+    o = _opts(ctx, stream)
+    _check(load().pcg_phi_batch(ax, aa, n, out, ctypes.byref(o)), ctx)
+    return list(out)

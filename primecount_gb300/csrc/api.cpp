@@ -1,0 +1,417 @@
+// api.cpp -- extern "C" boundary of libpcgpu and its host logic.
+//
+// Entry points mirror the reference's interfaces for the hard-leaf path
+// (see include/pcgpu.h for the file:line of each).  Errors never cross the
+// boundary as exceptions: every entry point returns a pcg_status and keeps
+// the message for pcg_last_error(), the way the reference's C API catches
+// primecount_error and prints it (src/api_c.cpp:19-30).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <chrono>
+#include <mutex>
+#include <thread>
+#include <algorithm>
+
+#include "pcg_internal.hpp"
+
+
+namespace pcg {
+
+// ---------------------------------------------------------------- errors
+struct Failure {
+  pcg_status status;
+  std::string msg;
+};
+
+void fail(pcg_status s, const std::string& msg) { throw Failure{s, msg}; }
+
+void cuda_check(cudaError_t e, const char* what)
+{
+  if (e == cudaSuccess) return;
+  cudaGetLastError();
+  pcg_status s = (e == cudaErrorMemoryAllocation) ? PCG_ENOMEM
+               : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) ? PCG_ENODEV : PCG_ECUDA;
+  fail(s, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+static thread_local std::string tl_error;
+
+// ---------------------------------------------------------------- integer math
+int64_t iroot(u128 x, int n)
+{
+  if (x == 0) return 0;
+  auto ipow = [](u128 r, int e) { u128 p = 1; for (int i = 0; i < e; i++) p *= r; return p; };
+  int64_t r = (int64_t) std::pow((double) x, 1.0 / n);
+  if (n == 2) r = (int64_t) std::sqrt((double) x);
+  if (n == 3) r = (int64_t) std::cbrt((double) x);
+  if (r < 0) r = 0;
+  for (; r > 0; r--)
+    if (ipow((u128) r, n - 1) <= x / (u128) r) break;
+  while (ipow((u128) (r + 1), n - 1) <= x / (u128) (r + 1)) r++;
+  return r;
+}
+
+std::string to_string(i128 v)
+{
+  if (v == 0) return "0";
+  bool neg = v < 0;
+  u128 u = neg ? (u128) (-(v + 1)) + 1 : (u128) v;
+  std::string s;
+  while (u) { s.push_back((char) ('0' + (int) (u % 10))); u /= 10; }
+  if (neg) s.push_back('-');
+  std::reverse(s.begin(), s.end());
+  return s;
+}
+
+Wheel2310::Wheel2310()
+{
+  int n = 0, last = -1;
+  for (int r = 0; r < 2310; r++) {
+    if (r % 2 && r % 3 && r % 5 && r % 7 && r % 11) { coprime[n] = (uint16_t) r; last = n; n++; }
+    index[r] = (int16_t) last;
+  }
+}
+
+const Wheel2310& wheel2310()
+{
+  static const Wheel2310 w;
+  return w;
+}
+
+// ---------------------------------------------------------------- parameters
+// Same formulas as the reference so that y, z, k are identical:
+// get_alpha_gourdon (src/util.cpp:276-349) and pi_gourdon_64/128
+// (src/gourdon/pi_gourdon.cpp:44-62).  The polynomial coefficients are the
+// reference's empirical tuning constants.
+static double in_between(double lo, double x, double hi) { return x < lo ? lo : (x > hi ? hi : x); }
+static double truncate3(double n) { return (double) ((int64_t) (n * 1000)) / 1000.0; }
+
+int64_t get_c(int64_t y)
+{
+  static const int64_t pi20[20] = {0, 0, 1, 2, 2, 3, 3, 4, 4, 4, 4, 5, 5, 6, 6, 6, 6, 7, 7, 8};
+  return (y >= 0 && y < 20) ? pi20[y] : 8;
+}
+
+int64_t x_star_gourdon(u128 x, int64_t y)
+{
+  y = std::max<int64_t>(y, 1);
+  u128 yy = (u128) y * (u128) y;
+  u128 x_div_yy = (x + yy - 1) / yy;
+  int64_t r4 = iroot(x, 4);
+  int64_t xs = (u128) r4 > x_div_yy ? r4 : (int64_t) x_div_yy;
+  int64_t sqrt_xy = isqrt(x / (u128) y);
+  xs = std::min(xs, y);
+  xs = std::min(xs, sqrt_xy);
+  return std::max<int64_t>(xs, 1);
+}
+
+GourdonParams gourdon_params(u128 x)
+{
+  double x16 = (double) iroot(x, 6);
+  double logx = std::log((double) x);
+  double alpha_yz;
+  if (x <= (u128) 100000000000ull)
+    alpha_yz = 0.078173 * logx + 1;
+  else {
+    const double a = 0.007888745747017503, b = -0.7610431057184933;
+    const double c = 25.74106177417062, d = -288.9823576050215;
+    alpha_yz = a * logx * logx * logx + b * logx * logx + c * logx + d;
+  }
+  double alpha_z = in_between(1, alpha_yz / 5, 1.0);
+  double alpha_y = alpha_yz / alpha_z;
+  alpha_y = in_between(1, alpha_y, x16);
+  alpha_y = truncate3(alpha_y);
+  alpha_z = truncate3(alpha_z);
+  alpha_y = in_between(1, alpha_y, x16);
+  double max_alpha_z = std::max(1.0, x16 / alpha_y);
+  alpha_z = in_between(1, alpha_z, max_alpha_z);
+
+  int64_t x13 = iroot(x, 3);
+  int64_t sqrtx = isqrt(x);
+  int64_t y = (int64_t) (x13 * alpha_y);
+  y = std::max(y, x13 + 1);
+  y = std::min(y, sqrtx - 1);
+  y = std::max<int64_t>(y, 1);
+  int64_t k = get_c(iroot(x, 4));
+  int64_t z = (int64_t) (y * alpha_z);
+  z = std::max(z, y);
+  z = std::min(z, sqrtx - 1);
+  z = std::max<int64_t>(z, 1);
+  GourdonParams p;
+  p.y = y;
+  p.z = z;
+  p.k = k;
+  p.x_star = x_star_gourdon(x, y);
+  return p;
+}
+
+DrParams dr_params(u128 x)
+{
+  double x16 = (double) iroot(x, 6);
+  double logx = std::log((double) x);
+  double alpha;
+  if (x <= (u128) 1000000000ull)
+    alpha = 0.078173 * logx + 1;
+  else
+    alpha = 0.00148918 * logx * logx * logx - 0.0691909 * logx * logx + 1.00165 * logx + 0.372253;
+  alpha = in_between(1, alpha, x16);
+  alpha = truncate3(alpha);
+  alpha = in_between(1, alpha, x16);
+  DrParams p;
+  p.y = (int64_t) (iroot(x, 3) * alpha);
+  p.z = (int64_t) (x / (u128) std::max<int64_t>(p.y, 1));
+  p.c = get_c(p.y);
+  return p;
+}
+
+// ---------------------------------------------------------------- contexts
+Ctx::~Ctx()
+{
+  for (auto& e : ev) if (e) cudaEventDestroy(e);
+  if (own_stream && stream) cudaStreamDestroy(stream);
+}
+
+static void ctx_init(Ctx& c)
+{
+  int dev = 0;
+  PCG_CUDA(cudaGetDevice(&dev));
+  c.device = dev;
+  PCG_CUDA(cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, dev));
+  int optin = 0;
+  PCG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  c.smem_optin = (size_t) optin;
+  PCG_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+  c.own_stream = true;
+  for (auto& e : c.ev) PCG_CUDA(cudaEventCreate(&e));
+}
+
+static std::mutex g_ctx_mu;
+static Ctx* g_default[64] = {nullptr};
+
+Ctx& default_ctx()
+{
+  int dev = 0;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    fail(PCG_ENODEV, "no CUDA device: libpcgpu computes on the GPU only");
+  }
+  PCG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> g(g_ctx_mu);
+  if (!g_default[dev]) {
+    Ctx* c = new Ctx();
+    ctx_init(*c);
+    g_default[dev] = c;
+  }
+  return *g_default[dev];
+}
+
+Ctx* ctx_from(const pcg_opts* o) { return (o && o->ctx) ? (Ctx*) o->ctx : &default_ctx(); }
+cudaStream_t stream_from(Ctx& c, const pcg_opts* o) { return (o && o->stream) ? (cudaStream_t) o->stream : c.stream; }
+
+}  // namespace pcg
+
+using namespace pcg;
+
+// The opaque handle is the Ctx itself.
+struct pcg_ctx : public Ctx {};
+
+template <class F>
+static pcg_status guard(Ctx* c, F&& f)
+{
+  try {
+    f();
+    return PCG_OK;
+  } catch (const Failure& e) {
+    tl_error = e.msg;
+    if (c) c->last_error = e.msg;
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    tl_error = "host allocation failed";
+    if (c) c->last_error = tl_error;
+    return PCG_ENOMEM;
+  } catch (const std::exception& e) {
+    tl_error = e.what();
+    if (c) c->last_error = tl_error;
+    return PCG_EINTERNAL;
+  }
+}
+
+static Tuning tuning_from(const pcg_opts* o)
+{
+  Tuning t;
+  if (o) {
+    t.segment_words = o->segment_words;
+    t.ctas_per_sm = o->ctas_per_sm;
+  }
+  return t;
+}
+
+static void print_result(const char* name, i128 v, double ms)
+{
+  std::printf("%s = %s\nSeconds: %.3f\n", name, to_string(v).c_str(), ms / 1000.0);
+}
+
+// checks of D.cpp:425-505 / FactorTableD.hpp:82-83 / main.cpp:224-229
+static void check_hard_args(u128 x, int64_t y, int64_t z, int64_t k, bool gourdon)
+{
+  if (y < 1 || z < 1 || k < 0) fail(PCG_EINVAL, "y, z must be >= 1 and k >= 0");
+  if (x > ((u128) y << 62)) fail(PCG_ERANGE, gourdon ? "D(x): x is too large" : "S2_hard(x): x is too large");
+  if (gourdon && z > 386083ll * 386083 - 1 && false) fail(PCG_ERANGE, "z must be <= FactorTableD::max()");
+}
+
+extern "C" {
+
+pcg_status pcg_ctx_create(pcg_i128 max_x, uint64_t mem_budget, pcg_ctx** out)
+{
+  if (!out) return PCG_EINVAL;
+  *out = nullptr;
+  pcg_ctx* c = nullptr;
+  pcg_status s = guard(nullptr, [&] {
+    if (max_x.hi < 0) fail(PCG_EINVAL, "max_x must be >= 0");
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+      cudaGetLastError();
+      fail(PCG_ENODEV, "no CUDA device: libpcgpu computes on the GPU only");
+    }
+    c = new pcg_ctx();
+    ctx_init(*c);
+    size_t free_b = 0, total_b = 0;
+    PCG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    c->mem_budget = mem_budget ? mem_budget : (uint64_t) (free_b * 0.9);
+    u128 x = make_u128(max_x);
+    if (x >= 10) {
+      GourdonParams g = gourdon_params(x);
+      ensure_prime_tables(*c, std::max<int64_t>(g.y, isqrt(x) / 1 > 0 ? g.y : g.y), c->stream);
+      ensure_factor_d(*c, g.z, g.z, c->stream);
+      if (pcg_ctx_device_bytes(c) > c->mem_budget)
+        fail(PCG_ENOMEM, "resident tables exceed the memory budget");
+    }
+  });
+  if (s != PCG_OK) {
+    delete c;
+    return s;
+  }
+  *out = c;
+  return PCG_OK;
+}
+
+void pcg_ctx_destroy(pcg_ctx* c) { delete c; }
+
+const char* pcg_last_error(const pcg_ctx* c)
+{
+  if (c) return c->last_error.c_str();
+  return tl_error.c_str();
+}
+
+uint64_t pcg_ctx_device_bytes(const pcg_ctx* c)
+{
+  if (!c) return 0;
+  const Tables& t = c->tab;
+  return t.primes.bytes + t.pitab.bytes + t.factor_d.bytes + t.factor_dr.bytes + t.coprime.bytes + t.cindex.bytes;
+}
+
+pcg_status pcg_last_stats(const pcg_ctx* c, pcg_stats* out)
+{
+  if (!out) return PCG_EINVAL;
+  return guard(nullptr, [&] {
+    const Ctx* cc = c ? (const Ctx*) c : &default_ctx();
+    *out = cc->last;
+  });
+}
+
+pcg_status pcg_gourdon_params(pcg_i128 xi, int64_t* y, int64_t* z, int64_t* k, int64_t* x_star)
+{
+  return guard(nullptr, [&] {
+    if (xi.hi < 0) fail(PCG_EINVAL, "x must be >= 0");
+    GourdonParams g = gourdon_params(make_u128(xi));
+    if (y) *y = g.y;
+    if (z) *z = g.z;
+    if (k) *k = g.k;
+    if (x_star) *x_star = g.x_star;
+  });
+}
+
+pcg_status pcg_dr_params(pcg_i128 xi, int64_t* y, int64_t* z, int64_t* c)
+{
+  return guard(nullptr, [&] {
+    if (xi.hi < 0) fail(PCG_EINVAL, "x must be >= 0");
+    DrParams d = dr_params(make_u128(xi));
+    if (y) *y = d.y;
+    if (z) *z = d.z;
+    if (c) *c = d.c;
+  });
+}
+
+static pcg_status hard_leaves(bool gourdon, pcg_i128 xi, int64_t y, int64_t z, int64_t k,
+                              const pcg_opts* opts, pcg_i128* out)
+{
+  if (!out) return PCG_EINVAL;
+  Ctx* cp = nullptr;
+  return guard(nullptr, [&] {
+    cp = ctx_from(opts);
+    Ctx& c = *cp;
+    c.last_error.clear();
+    if (xi.hi < 0) fail(PCG_EINVAL, "x must be >= 0");
+    u128 x = make_u128(xi);
+    i128 result = 0;
+    if (x >= 1) {
+      check_hard_args(x, y, z, k, gourdon);
+      SweepProblem p;
+      p.gourdon = gourdon ? 1 : 0;
+      p.x = x;
+      p.y = y;
+      p.z = z;
+      p.k = k;
+      SweepResult r = run_sweep(c, p, tuning_from(opts), stream_from(c, opts));
+      result = r.sum;
+      c.last = r.stats;
+      if (opts && opts->print) print_result(gourdon ? "D" : "S2_hard", result, r.stats.total_ms);
+    }
+    *out = to_pcg(result);
+  });
+}
+
+pcg_status pcg_D(pcg_i128 x, int64_t y, int64_t z, int64_t k, const pcg_opts* opts, pcg_i128* out)
+{
+  return hard_leaves(true, x, y, z, k, opts, out);
+}
+
+pcg_status pcg_S2_hard(pcg_i128 x, int64_t y, int64_t z, int64_t c, const pcg_opts* opts, pcg_i128* out)
+{
+  return hard_leaves(false, x, y, z, c, opts, out);
+}
+
+pcg_status pcg_D_default(pcg_i128 xi, const pcg_opts* opts, pcg_i128* out, int64_t* y, int64_t* z, int64_t* k)
+{
+  int64_t yy = 1, zz = 1, kk = 0, xs = 0;
+  if (xi.hi < 0 || (xi.hi == 0 && xi.lo < 1)) {
+    if (out) *out = to_pcg(0);
+    return xi.hi < 0 ? PCG_EINVAL : PCG_OK;
+  }
+  pcg_status s = pcg_gourdon_params(xi, &yy, &zz, &kk, &xs);
+  if (s != PCG_OK) return s;
+  if (y) *y = yy;
+  if (z) *z = zz;
+  if (k) *k = kk;
+  return pcg_D(xi, yy, zz, kk, opts, out);
+}
+
+pcg_status pcg_S2_hard_default(pcg_i128 xi, const pcg_opts* opts, pcg_i128* out, int64_t* y, int64_t* z, int64_t* c)
+{
+  int64_t yy = 1, zz = 1, cc = 0;
+  if (xi.hi < 0 || (xi.hi == 0 && xi.lo < 1)) {
+    if (out) *out = to_pcg(0);
+    return xi.hi < 0 ? PCG_EINVAL : PCG_OK;
+  }
+  pcg_status s = pcg_dr_params(xi, &yy, &zz, &cc);
+  if (s != PCG_OK) return s;
+  if (y) *y = yy;
+  if (z) *z = zz;
+  if (c) *c = cc;
+  return pcg_S2_hard(xi, yy, zz, cc, opts, out);
+}
+
+}  // extern "C"

@@ -1,0 +1,143 @@
+// pcg_internal.hpp -- host-side declarations shared by the engine sources.
+//
+// The engine evaluates the hard special leaves of Gourdon's D(x, y, z, k)
+// (reference: src/gourdon/D.cpp) and Deleglise-Rivat's S2_hard(x, y, z, c)
+// (reference: src/deleglise-rivat/S2_hard.cpp) with one CUDA sweep over the
+// sieve interval.  See sweep.cu for the device side.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "pcgpu.h"
+
+namespace pcg {
+
+typedef unsigned __int128 u128;
+typedef __int128 i128;
+
+// ---------------------------------------------------------------- errors
+struct Error {
+  pcg_status status;
+  std::string msg;
+};
+
+// Throwing helpers are internal only: every extern "C" entry point catches.
+[[noreturn]] void fail(pcg_status s, const std::string& msg);
+void cuda_check(cudaError_t e, const char* what);
+#define PCG_CUDA(call) ::pcg::cuda_check((call), #call)
+
+// ---------------------------------------------------------------- integer math
+int64_t iroot(u128 x, int n);            // exact floor(x^(1/n)), n in {2,3,4,6}
+inline int64_t isqrt(u128 x) { return iroot(x, 2); }
+inline u128 make_u128(pcg_i128 v) { return ((u128) (uint64_t) v.hi << 64) | v.lo; }
+inline pcg_i128 to_pcg(i128 v) { pcg_i128 r; r.lo = (uint64_t) v; r.hi = (int64_t) (v >> 64); return r; }
+std::string to_string(i128 v);
+
+// 2*3*5*7*11 wheel of the FactorTables (reference src/BaseFactorTable.hpp:36-47)
+struct Wheel2310 {
+  uint16_t coprime[480];     // numbers in [0, 2310) coprime to 2..11, ascending
+  int16_t index[2310];       // index of the largest coprime <= r (-1 for r = 0)
+  Wheel2310();
+  int64_t to_index(uint64_t n) const { return 480 * (int64_t) (n / 2310) + index[n % 2310]; }
+  int64_t to_number(uint64_t i) const { return 2310 * (int64_t) (i / 480) + coprime[i % 480]; }
+};
+const Wheel2310& wheel2310();
+
+// ---------------------------------------------------------------- parameters
+struct GourdonParams { int64_t y, z, k, x_star; };
+struct DrParams { int64_t y, z, c; };
+GourdonParams gourdon_params(u128 x);    // src/gourdon/pi_gourdon.cpp:44-62
+DrParams dr_params(u128 x);              // src/app/main.cpp:435-461
+int64_t x_star_gourdon(u128 x, int64_t y);   // src/util.cpp:362-386
+int64_t get_c(int64_t y);                // src/PhiTiny.hpp:47-50
+
+// ---------------------------------------------------------------- device buffers
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  ~DevBuf();
+  void alloc(size_t n);
+  void free_();
+  template <class T> T* as() const { return (T*) p; }
+};
+
+// Device-resident tables of one context.
+struct Tables {
+  // primes (uint32, 1-indexed, primes[0] = 0) and PiTable {count, bits} per 240
+  int64_t prime_limit = -1;  // tables cover [0, prime_limit]
+  int64_t nprimes = 0;
+  DevBuf primes;             // uint32[nprimes + 2]
+  DevBuf pitab;              // uint64[2 * (prime_limit / 240 + 1)]
+  std::vector<uint32_t> h_primes;   // host copy of the primes (small part)
+  std::vector<uint64_t> h_pitab;    // host copy of the PiTable
+  // FactorTableD (Gourdon): entries for coprime-to-2310 n <= fd_z, mpf filter fd_y
+  int64_t fd_y = -1, fd_z = -1;
+  int fd_bytes = 2;          // 2 = uint16_t entries, 4 = uint32_t
+  DevBuf factor_d;
+  // FactorTable (Deleglise-Rivat): n <= fr_y
+  int64_t fr_y = -1;
+  int fr_bytes = 2;
+  DevBuf factor_dr;
+  // wheel tables on device
+  DevBuf coprime;            // uint16[480]
+  DevBuf cindex;             // int16[2310]
+  double build_ms = 0;
+};
+
+struct Ctx;
+
+// Builds (or reuses) the prime tables up to `limit`.
+void ensure_prime_tables(Ctx& c, int64_t limit, cudaStream_t s);
+// FactorTableD for (y, z); FactorTable (DR) for y.
+void ensure_factor_d(Ctx& c, int64_t y, int64_t z, cudaStream_t s);
+void ensure_factor_dr(Ctx& c, int64_t y, cudaStream_t s);
+
+// host PiTable lookup on the host copy
+int64_t host_pi(const Tables& t, uint64_t x);
+
+// ---------------------------------------------------------------- sweep
+struct SweepProblem {
+  int gourdon;         // 1: D, 0: S2_hard
+  u128 x;
+  int64_t y, z, k;     // k = c for S2_hard
+};
+
+struct Tuning {
+  int segment_words = 0;
+  int ctas_per_sm = 0;
+};
+
+struct SweepResult {
+  i128 sum = 0;
+  pcg_stats stats{};
+};
+
+SweepResult run_sweep(Ctx& c, const SweepProblem& p, const Tuning& t, cudaStream_t s);
+
+// ---------------------------------------------------------------- context
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int num_sms = 0;
+  size_t smem_optin = 0;
+  uint64_t mem_budget = 0;
+  Tables tab;
+  // scratch of the sweep (grown on demand)
+  DevBuf cnt, smu, segsum, run, acc, misc;
+  pcg_stats last{};
+  std::string last_error;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  ~Ctx();
+};
+
+Ctx& default_ctx();
+Ctx* ctx_from(const pcg_opts* o);
+cudaStream_t stream_from(Ctx& c, const pcg_opts* o);
+
+}  // namespace pcg

@@ -1,0 +1,1074 @@
+// sweep.cu -- sm_103a kernels of the hard-special-leaf engine.
+//
+// What is computed (reference semantics):
+//   D(x, y, z, k)      src/gourdon/D.cpp:69-308 (D_thread_default)
+//   S2_hard(x, y, z, c) src/deleglise-rivat/S2_hard.cpp:51-161
+// Both are sums over "hard special leaves" n = x / (p_b * m) that fall in the
+// sieve interval [0, L):  -mu(m) * phi(n, b-1)  (m square-free, lpf(m) > p_b)
+// and  +phi(n, b-1) for n = x / (p_b * p_l).
+//
+// How (GB300 design, not the reference's):
+//  * The interval is cut into segments of `words` 64-bit words; each word
+//    holds the 64 numbers coprime to 30 of a block of 240 (the reference's
+//    BitSieve240 layout, src/sieve/Sieve.hpp:8-12).  One CTA owns one
+//    segment in shared memory and sieves it level by level, b = 1, 2, ...
+//  * phi(n, b-1) = phi(low-1, b-1) + (# unsieved in [low, n]).  The first
+//    term is the only thing that couples segments, and a leaf's contribution
+//    is linear in it.  So each (segment, b) records
+//        C(s, b)  = # numbers of the segment left after sieving p_1..p_{b-1}
+//        M(s, b)  = sum over its leaves of the sign (-mu(m) or +1)
+//    and the local counts are summed directly.  A scan over segments then
+//    adds sum_b sum_s M(s, b) * sum_{s'<s} C(s', b).  This replaces the
+//    reference's per-chunk phi_vector (src/phi_vector.cpp:302-336) and makes
+//    every segment independent: no second sieve pass is needed.
+//  * Leaf queries are random-order popcount prefix queries against a
+//    per-64-word chunk prefix array rebuilt (block scan) only when the
+//    bitmap changed since the last leaf level.
+//  * Segments are handed out by an atomic counter (device work queue, the
+//    role of LoadBalancerS2, src/LoadBalancerS2.cpp:139-193) in waves whose
+//    C/M matrices fit a fixed HBM budget.
+#include <cstdio>
+#include <cstring>
+#include <chrono>
+#include <algorithm>
+
+#include "pcg_internal.hpp"
+
+namespace pcg {
+
+// ---------------------------------------------------------------- constants
+// # of wheel offsets {1,7,11,13,17,19,23,29} that are <= t, for t in [0, 30):
+// nibble t of these two words.
+#define PCG_CNT8_LO 0x4443322221111110ull
+#define PCG_CNT8_HI 0x0087777776666554ull
+// wheel offsets packed as bytes
+#define PCG_WOFF 0x1D1713110D0B0701ull
+
+__device__ __forceinline__ uint32_t cnt8(uint32_t t)
+{
+  uint64_t v = t < 16 ? PCG_CNT8_LO : PCG_CNT8_HI;
+  uint32_t sh = (t < 16 ? t : t - 16) * 4;
+  return (uint32_t) (v >> sh) & 15u;
+}
+
+// bits of a 240-block for the numbers <= r (r in [0, 240))
+__device__ __forceinline__ uint64_t mask_le(uint32_t r)
+{
+  uint32_t byte = r / 30;
+  uint32_t nb = byte * 8 + cnt8(r - byte * 30);
+  return nb >= 64 ? ~0ull : ((1ull << nb) - 1);
+}
+
+__device__ __forceinline__ uint32_t woff(uint32_t j) { return (uint32_t) (PCG_WOFF >> (8 * j)) & 0xFFu; }
+
+// # numbers in [1, q] coprime to 30
+__device__ __forceinline__ uint64_t cnt_le(uint64_t q) { return 8 * (q / 30) + cnt8((uint32_t) (q % 30)); }
+
+// bit of number offset `off` (coprime to 30) inside its word
+__device__ __forceinline__ uint32_t bit_of(uint32_t r) { return (r / 30) * 8 + cnt8(r % 30) - 1; }
+
+// PiTable lookup: {count, bits} per 240 numbers (count includes 2, 3, 5)
+__device__ __forceinline__ int64_t dpi(const uint64_t* __restrict__ pt, uint64_t x)
+{
+  if (x < 6) return (0x322100u >> (4 * x)) & 15u;
+  uint64_t i = x / 240;
+  return (int64_t) (pt[2 * i] + __popcll(pt[2 * i + 1] & mask_le((uint32_t) (x - 240 * i))));
+}
+
+__device__ __forceinline__ int64_t dmin(int64_t a, int64_t b) { return a < b ? a : b; }
+__device__ __forceinline__ int64_t dmax(int64_t a, int64_t b) { return a > b ? a : b; }
+
+// exact floor(sqrt(x)) for x < 2^126
+__device__ int64_t disqrt(u128 x)
+{
+  if (x == 0) return 0;
+  int64_t r = (int64_t) sqrt((double) x);
+  while (r > 0 && (u128) r * (u128) r > x) r--;
+  while ((u128) (r + 1) * (u128) (r + 1) <= x) r++;
+  return r;
+}
+
+// min(floor(a / d), cap) for d >= 1, cap >= 0
+__device__ __forceinline__ int64_t divcap(u128 a, uint64_t d, int64_t cap)
+{
+  if ((u128) d * (u128) cap <= a) return cap;
+  return (int64_t) (a / d);
+}
+
+// ================================================================ prime tables
+// PiTable bits: word w holds the primes >= 7 among 240w + {1,7,...}
+__global__ void k_prime_bits(uint64_t* __restrict__ out_bits, uint32_t* __restrict__ out_pc,
+                             int64_t nwords, int64_t limit,
+                             const uint32_t* __restrict__ base, int nbase)
+{
+  extern __shared__ uint64_t sb[];
+  const int WB = 2048;
+  int64_t w0 = (int64_t) blockIdx.x * WB;
+  int64_t wn = dmin(WB, nwords - w0);
+  uint64_t lo = (uint64_t) w0 * 240;
+  uint64_t hi = lo + (uint64_t) wn * 240;   // [lo, hi)
+  for (int i = threadIdx.x; i < wn; i += blockDim.x) {
+    uint64_t v = ~0ull;
+    uint64_t wl = lo + (uint64_t) i * 240;
+    if (wl + 239 > (uint64_t) limit) v = ((uint64_t) limit >= wl) ? mask_le((uint32_t) (limit - wl)) : 0;
+    if (w0 + i == 0) v &= ~1ull;            // 1 is not prime
+    sb[i] = v;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = warp; k < nbase; k += nw) {
+    uint64_t p = base[k];
+    if (p * p >= hi) break;
+    uint64_t qlo = (lo + p - 1) / p;
+    if (qlo < p) qlo = p;
+    uint64_t qhi = (hi - 1) / p;
+    if (qlo > qhi) continue;
+    uint64_t jlo = cnt_le(qlo - 1), jhi = cnt_le(qhi);
+    for (uint64_t j = jlo + lane; j < jhi; j += 32) {
+      uint64_t q = 30 * (j >> 3) + woff((uint32_t) (j & 7));
+      uint32_t off = (uint32_t) (p * q - lo);
+      uint32_t w = off / 240, r = off - w * 240;
+      atomicAnd((unsigned long long*) &sb[w], ~(1ull << bit_of(r)));
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < wn; i += blockDim.x) {
+    out_bits[w0 + i] = sb[i];
+    out_pc[w0 + i] = __popcll(sb[i]);
+  }
+}
+
+// ---- exclusive scan uint32 -> uint64 (three phases)
+#define SCAN_ITEMS 4096
+__global__ void k_scan_sums(const uint32_t* __restrict__ in, int64_t n, uint64_t* __restrict__ sums)
+{
+  __shared__ uint64_t red[32];
+  int64_t base = (int64_t) blockIdx.x * SCAN_ITEMS;
+  uint64_t s = 0;
+  for (int i = threadIdx.x; i < SCAN_ITEMS; i += blockDim.x)
+    if (base + i < n) s += in[base + i];
+  for (int d = 16; d > 0; d >>= 1) s += __shfl_down_sync(0xffffffffu, s, d);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint64_t t = 0;
+    for (int i = 0; i < (int) (blockDim.x >> 5); i++) t += red[i];
+    sums[blockIdx.x] = t;
+  }
+}
+
+__global__ void k_scan_serial(uint64_t* sums, int64_t n)
+{
+  // one block: exclusive scan of n block sums (n is small)
+  __shared__ uint64_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int64_t base = 0; base < n; base += blockDim.x) {
+    int64_t i = base + threadIdx.x;
+    uint64_t v = i < n ? sums[i] : 0;
+    // inclusive warp scan then block scan
+    __shared__ uint64_t wt[32];
+    uint64_t incl = v;
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int d = 1; d < 32; d <<= 1) {
+      uint64_t t = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += t;
+    }
+    if (lane == 31) wt[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+      uint64_t a = lane < (int) (blockDim.x >> 5) ? wt[lane] : 0;
+      uint64_t ai = a;
+      for (int d = 1; d < 32; d <<= 1) {
+        uint64_t t = __shfl_up_sync(0xffffffffu, ai, d);
+        if (lane >= d) ai += t;
+      }
+      wt[lane] = ai - a;
+    }
+    __syncthreads();
+    uint64_t excl = carry + wt[warp] + incl - v;
+    if (i < n) sums[i] = excl;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+    __syncthreads();
+  }
+}
+
+__global__ void k_scan_apply(const uint32_t* __restrict__ in, int64_t n, const uint64_t* __restrict__ sums,
+                             uint64_t* __restrict__ out)
+{
+  // blockDim.x == 512, 8 items per thread, contiguous
+  __shared__ uint64_t wt[16];
+  int64_t base = (int64_t) blockIdx.x * SCAN_ITEMS + threadIdx.x * 8;
+  uint32_t v[8];
+  uint64_t s = 0;
+  for (int i = 0; i < 8; i++) { v[i] = (base + i < n) ? in[base + i] : 0; s += v[i]; }
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint64_t incl = s;
+  for (int d = 1; d < 32; d <<= 1) {
+    uint64_t t = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += t;
+  }
+  if (lane == 31) wt[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint64_t a = lane < 16 ? wt[lane] : 0, ai = a;
+    for (int d = 1; d < 32; d <<= 1) {
+      uint64_t t = __shfl_up_sync(0xffffffffu, ai, d);
+      if (lane >= d) ai += t;
+    }
+    if (lane < 16) wt[lane] = ai - a;
+  }
+  __syncthreads();
+  uint64_t run = sums[blockIdx.x] + wt[warp] + incl - s;
+  for (int i = 0; i < 8; i++) {
+    if (base + i < n) out[base + i] = run;
+    run += v[i];
+  }
+}
+
+// pitab[2w] = 3 + #primes>=7 below 240w, pitab[2w+1] = bits; primes compaction
+__global__ void k_pitab_primes(const uint64_t* __restrict__ bits, const uint64_t* __restrict__ excl,
+                               int64_t nwords, uint64_t* __restrict__ pitab, uint32_t* __restrict__ primes)
+{
+  int64_t w = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nwords) return;
+  uint64_t b = bits[w];
+  uint64_t e = excl[w];
+  pitab[2 * w] = 3 + e;
+  pitab[2 * w + 1] = b;
+  uint64_t idx = 4 + e;   // primes[1..3] = 2, 3, 5
+  while (b) {
+    int j = __ffsll((long long) b) - 1;
+    b &= b - 1;
+    primes[idx++] = (uint32_t) (240 * (uint64_t) w + 30 * (j >> 3) + woff(j & 7));
+  }
+}
+
+// ================================================================ factor tables
+// Entries for n = to_number(i) coprime to 2310 (reference layout,
+// src/BaseFactorTable.hpp:36-47).  gourdon = 1 builds FactorTableD
+// (src/gourdon/FactorTableD.hpp:20-39): 2*pi(lpf) + [mu = -1], T_MAX for a
+// prime <= y, T_MAX - 1 for 1, 0 if mu = 0 or a prime factor > y.
+// gourdon = 0 builds the Deleglise-Rivat FactorTable (src/FactorTable.hpp:
+// 154-166): lpf if mu = -1, lpf - 1 if mu = 1, T_MAX for primes, 0 if mu = 0.
+// Method: per block of E entries, every prime p <= sqrt(limit) marks its
+// multiples p*q (q coprime to 2310) with shared-memory atomics: minimum
+// prime index, product of distinct small primes, factor count and a square
+// flag; the cofactor n / product is then the one prime factor > sqrt(limit).
+#define FT_E 4096
+template <typename T>
+__global__ void k_factor(T* __restrict__ out, int64_t size, int64_t limit, int64_t y, int gourdon,
+                         const uint32_t* __restrict__ primes, int64_t nsmall,
+                         const uint16_t* __restrict__ g_coprime, const int16_t* __restrict__ g_cindex)
+{
+  extern __shared__ __align__(16) unsigned char fsm[];
+  unsigned long long* prod = (unsigned long long*) fsm;
+  uint32_t* lpfi = (uint32_t*) (prod + FT_E);
+  uint32_t* nf = lpfi + FT_E;          // bits 0..7 count, bit 30 square, bits 8..29 max prime index
+  uint16_t* cop = (uint16_t*) (nf + FT_E);
+  int16_t* cid = (int16_t*) (cop + 480);
+  for (int i = threadIdx.x; i < 480; i += blockDim.x) cop[i] = g_coprime[i];
+  for (int i = threadIdx.x; i < 2310; i += blockDim.x) cid[i] = g_cindex[i];
+  int64_t i0 = (int64_t) blockIdx.x * FT_E;
+  int64_t en = dmin(FT_E, size - i0);
+  for (int i = threadIdx.x; i < FT_E; i += blockDim.x) { prod[i] = 1; lpfi[i] = 0xFFFFFFFFu; nf[i] = 0; }
+  __syncthreads();
+  auto to_number = [&](uint64_t i) -> uint64_t { return 2310 * (i / 480) + cop[i % 480]; };
+  auto to_index = [&](uint64_t n) -> int64_t { return 480 * (int64_t) (n / 2310) + cid[n % 2310]; };
+  uint64_t nlo = to_number((uint64_t) i0), nhi = to_number((uint64_t) (i0 + en - 1));
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  // small primes: index 6 (p = 13) .. nsmall
+  for (int64_t k = 6 + warp; k <= nsmall; k += nw) {
+    uint64_t p = primes[k];
+    uint64_t qlo = (nlo + p - 1) / p;
+    uint64_t qhi = nhi / p;
+    if (qlo > qhi) continue;
+    int64_t jlo = (qlo <= 1) ? 0 : to_index(qlo - 1) + 1;
+    int64_t jhi = to_index(qhi);
+    for (int64_t j = jlo + lane; j <= jhi; j += 32) {
+      uint64_t q = to_number((uint64_t) j);
+      uint64_t n = p * q;
+      int64_t li = to_index(n) - i0;
+      atomicMin(&lpfi[li], (uint32_t) k);
+      atomicAdd(&nf[li], 1u);
+      if (q % p == 0) atomicOr(&nf[li], 1u << 30);
+      unsigned long long old = prod[li], assumed;
+      do {
+        assumed = old;
+        old = atomicCAS(&prod[li], assumed, assumed * p);
+      } while (old != assumed);
+    }
+  }
+  __syncthreads();
+  const uint64_t TMAX = sizeof(T) == 2 ? 0xFFFFull : 0xFFFFFFFFull;
+  for (int i = threadIdx.x; i < en; i += blockDim.x) {
+    uint64_t n = to_number((uint64_t) (i0 + i));
+    uint64_t v;
+    if (n == 1) v = TMAX ^ 1;
+    else {
+      uint64_t P = prod[i];
+      uint64_t large = n / P;
+      uint32_t cnt = (nf[i] & 0xFFu) + (large > 1 ? 1u : 0u);
+      bool sq = (nf[i] >> 30) & 1u;
+      if (sq) v = 0;
+      else if (cnt == 1) v = (gourdon && (int64_t) n > y) ? 0 : TMAX;   // n is prime
+      else if (gourdon && (int64_t) large > y) v = 0;
+      else {
+        uint32_t li = lpfi[i];
+        if (gourdon) {
+          v = 2 * (uint64_t) li + (cnt & 1);
+        } else {
+          uint64_t lpf = primes[li];
+          v = (cnt & 1) ? lpf : lpf - 1;
+        }
+      }
+    }
+    out[i0 + i] = (T) v;
+  }
+}
+
+// Small primes > y (possible only when sqrt(z) > y): zero their multiples.
+template <typename T>
+__global__ void k_factor_zero_small(T* __restrict__ out, int64_t size, int64_t limit,
+                                    const uint32_t* __restrict__ primes, int64_t k_first, int64_t k_last,
+                                    const uint16_t* __restrict__ g_coprime, const int16_t* __restrict__ g_cindex)
+{
+  int64_t k = k_first + blockIdx.x;
+  if (k > k_last) return;
+  uint64_t p = primes[k];
+  for (int64_t j = threadIdx.x; ; j += blockDim.x) {
+    uint64_t q = 2310 * (j / 480) + g_coprime[j % 480];
+    uint64_t n = p * q;
+    if ((int64_t) n > limit) break;
+    int64_t li = 480 * (int64_t) (n / 2310) + g_cindex[n % 2310];
+    if (li < size) out[li] = 0;
+  }
+}
+
+// ================================================================ the sweep
+struct LevelP {
+  int64_t lo, hi;     // leaf range (lo, hi]: factor indices (family 1) or prime indices (family 2)
+  uint64_t jlo;       // first 30-coprime rank of the cross-off co-factors
+  uint32_t jn;        // number of cross-off co-factors
+  uint32_t prime;
+  uint32_t thr;       // factor-table threshold (family 1)
+  uint32_t flags;     // 1: leaves, 2: family 2
+};
+
+struct SweepArgs {
+  uint64_t x_lo, x_hi;
+  int64_t y, z, k, L, x_star;
+  int64_t seg;           // numbers per segment = words * 240
+  int32_t words;
+  int32_t gourdon;
+  int32_t pi_sqrt;       // last level of family 1
+  int32_t bglob;         // columns = bglob + 1
+  int64_t wave_first;
+  int32_t wave_len;
+  int32_t pad0;
+  const uint32_t* primes;
+  int64_t nprimes;
+  const uint64_t* pitab;
+  int64_t pi_max;
+  const void* factor;
+  const uint64_t* xp_tab;   // [bglob+1][3]: x/p lo, hi, min(x/p^3, 2^63-1)
+  const uint16_t* coprime;
+  const int16_t* cindex;
+  uint32_t* cnt;            // [wave_len][bglob+1]
+  int32_t* smu;             // [wave_len][bglob+1]
+  int64_t* segsum;          // [wave_len]
+  unsigned long long* counters;  // [0] leaves, [1] two-prime leaves, [2] levels, [3] factor entries
+  int* queue;
+};
+
+// x / m for m < 2^32 when the quotient is known to fit in 63 bits
+__device__ __forceinline__ uint64_t div_xp32(uint64_t xlo, uint64_t xhi, uint32_t m)
+{
+  if (xhi == 0) return xlo / m;
+  uint64_t t = (xhi << 32) | (xlo >> 32);
+  uint64_t q1 = t / m;
+  uint64_t r = t - q1 * m;
+  uint64_t t2 = (r << 32) | (xlo & 0xFFFFFFFFull);
+  return (q1 << 32) | (t2 / m);
+}
+
+__device__ __forceinline__ uint64_t div_xp(uint64_t xlo, uint64_t xhi, uint64_t m)
+{
+  if (m <= 0xFFFFFFFFull) return div_xp32(xlo, xhi, (uint32_t) m);
+  u128 xp = ((u128) xhi << 64) | xlo;
+  return (uint64_t) (xp / m);
+}
+
+template <int NT>
+__device__ __forceinline__ void block_scan_chunks(const uint32_t* __restrict__ ccount, uint32_t* __restrict__ pref,
+                                                  int nch, uint32_t* wtmp)
+{
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int cpt = nch / NT;      // nch is a multiple of NT
+  int base = tid * cpt;
+  uint32_t s = 0;
+  for (int c = 0; c < cpt; c++) s += ccount[base + c];
+  uint32_t incl = s;
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += t;
+  }
+  if (lane == 31) wtmp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t a = lane < NT / 32 ? wtmp[lane] : 0, ai = a;
+    for (int d = 1; d < 32; d <<= 1) {
+      uint32_t t = __shfl_up_sync(0xffffffffu, ai, d);
+      if (lane >= d) ai += t;
+    }
+    if (lane < NT / 32) wtmp[lane] = ai - a;
+  }
+  __syncthreads();
+  uint32_t run = wtmp[warp] + incl - s;
+  for (int c = 0; c < cpt; c++) {
+    pref[base + c] = run;
+    run += ccount[base + c];
+  }
+  __syncthreads();
+}
+
+// # unsieved numbers in [low, low + off]
+__device__ __forceinline__ uint32_t query(const uint64_t* __restrict__ bits, const uint32_t* __restrict__ pref,
+                                          uint32_t off)
+{
+  uint32_t w = off / 240;
+  uint32_t r = off - w * 240;
+  uint32_t c = w >> 3;
+  uint32_t v = pref[c];
+  for (uint32_t i = c << 3; i < w; i++) v += __popcll(bits[i]);
+  return v + __popcll(bits[w] & mask_le(r));
+}
+
+template <typename FT, int NT>
+__global__ void __launch_bounds__(NT) k_sweep(const SweepArgs A)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nch = A.words >> 3;
+  uint64_t* bits = (uint64_t*) smem_raw;
+  uint32_t* ccount = (uint32_t*) (bits + A.words);
+  uint32_t* pref = ccount + nch;
+  LevelP* lp = (LevelP*) (pref + nch);
+  uint16_t* cop = (uint16_t*) (lp + NT);
+
+  __shared__ int s_ws;
+  __shared__ int s_smu;
+  __shared__ int s_stop;
+  __shared__ uint32_t s_rem[3];
+  __shared__ uint32_t s_total;
+  __shared__ uint32_t wtmp[32];
+  __shared__ long long s_red[NT / 32];
+  __shared__ unsigned long long s_ctr[4];
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const FT* __restrict__ factor = (const FT*) A.factor;
+  const u128 x = ((u128) A.x_hi << 64) | A.x_lo;
+  const int cols = A.bglob + 1;
+  for (int i = tid; i < 480; i += NT) cop[i] = A.coprime[i];
+  if (tid < 4) s_ctr[tid] = 0;
+
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) s_ws = atomicAdd(A.queue, 1);
+    __syncthreads();
+    const int ws = s_ws;
+    if (ws >= A.wave_len) break;
+    const int64_t s = A.wave_first + ws;
+    const int64_t low = s * A.seg;
+    const int64_t high = dmin(low + A.seg, A.L);
+    const int64_t low1 = dmax(low, 1);
+
+    // level bounds of this segment (chunk bounds of D.cpp:83-94 / S2_hard.cpp:64-71)
+    int64_t bmin_leaf, bmax_leaf, bcnt;
+    if (A.gourdon) {
+      bmax_leaf = dpi(A.pitab, (uint64_t) dmin(dmin(disqrt(x / (uint64_t) low1), disqrt((u128) high)), A.x_star));
+      bmin_leaf = dpi(A.pitab, (uint64_t) dmin(A.L / high, A.x_star));
+      bcnt = dpi(A.pitab, (uint64_t) dmin(disqrt(x / (uint64_t) high), A.x_star));
+    } else {
+      bmax_leaf = (high <= A.y) ? A.pi_sqrt
+          : dpi(A.pitab, (uint64_t) dmin(dmin(disqrt(x / (uint64_t) low1), disqrt((u128) A.z)), A.y));
+      uint64_t pmax = bmax_leaf > 0 ? A.primes[bmax_leaf] : 0;
+      bmin_leaf = dpi(A.pitab, (uint64_t) dmin(A.z / high, (int64_t) pmax));
+      bcnt = dmax(A.pi_sqrt, dpi(A.pitab, (uint64_t) dmin(dmin(disqrt(x / (uint64_t) high), disqrt((u128) A.z)), A.y)));
+    }
+    bmin_leaf = dmax(A.k, bmin_leaf) + 1;
+    const int Bs = (int) dmin(dmax(bmax_leaf, bcnt), (int64_t) A.bglob);
+
+    // fill the segment: every number coprime to 30 in [low, high)
+    const uint32_t span = (uint32_t) (high - low);
+    const int wused = (int) ((span + 239) / 240);
+    for (int w = tid; w < A.words; w += NT) {
+      uint64_t v = w < wused ? ~0ull : 0ull;
+      if (w == wused - 1) v &= mask_le((span - 1) % 240);
+      bits[w] = v;
+    }
+    if (tid == 0) { s_total = 0; s_rem[0] = s_rem[1] = s_rem[2] = 0; s_smu = 0; s_stop = 0x7FFFFFFF; }
+    __syncthreads();
+    {
+      uint32_t part = 0;
+      for (int c = tid; c < nch; c += NT) {
+        uint32_t t = 0;
+        for (int i = 0; i < 8; i++) t += __popcll(bits[8 * c + i]);
+        ccount[c] = t;
+        part += t;
+      }
+      for (int d = 16; d > 0; d >>= 1) part += __shfl_down_sync(0xffffffffu, part, d);
+      if (lane == 0) atomicAdd(&s_total, part);
+    }
+    __syncthreads();
+    uint32_t total = s_total;
+    bool dirty = true;
+    long long lsum = 0;
+    unsigned long long nleaves = 0, ntwo = 0, nentries = 0;
+
+    for (int b0 = 1; b0 <= Bs; b0 += NT) {
+      // ---- per-level parameters of levels b0 .. b0+NT-1, one thread each
+      {
+        const int b = b0 + tid;
+        LevelP P;
+        P.lo = P.hi = 0; P.jlo = 0; P.jn = 0; P.prime = 0; P.thr = 0; P.flags = 0;
+        if (b <= Bs) {
+          const uint64_t p = A.primes[b];
+          P.prime = (uint32_t) p;
+          if (p >= 7) {
+            uint64_t qlo = ((uint64_t) low + p - 1) / p;
+            if (qlo < 1) qlo = 1;
+            uint64_t qhi = ((uint64_t) high - 1) / p;
+            if (qlo <= qhi) {
+              P.jlo = cnt_le(qlo - 1);
+              P.jn = (uint32_t) (cnt_le(qhi) - P.jlo);
+            }
+          }
+          if (b >= bmin_leaf && b <= bmax_leaf) {
+            const uint64_t* xt = A.xp_tab + 3 * b;
+            const u128 xp = ((u128) xt[1] << 64) | xt[0];
+            const int64_t xpp = (int64_t) xt[2];
+            const int64_t prime = (int64_t) p;
+            bool stop = false;
+            if (b <= A.pi_sqrt) {
+              int64_t min_m, max_m;
+              if (A.gourdon) {
+                int64_t xp_low = divcap(xp, (uint64_t) low1, A.z);
+                int64_t xp_high = divcap(xp, (uint64_t) high, A.z);
+                min_m = dmax(xp_high, A.z / prime);
+                max_m = dmin(xpp, xp_low);
+                P.thr = (uint32_t) (2 * b + 1);
+              } else {
+                int64_t xp_high = divcap(xp, (uint64_t) high, A.y);
+                min_m = dmax(xp_high, A.y / prime);
+                max_m = divcap(xp, (uint64_t) low1, A.y);
+                P.thr = (uint32_t) prime;
+              }
+              if (prime >= max_m) stop = true;
+              else {
+                P.lo = 480 * (min_m / 2310) + A.cindex[min_m % 2310];
+                P.hi = 480 * (max_m / 2310) + A.cindex[max_m % 2310];
+                if (P.hi > P.lo) P.flags = 1;
+              }
+            } else {
+              int64_t xp_low = divcap(xp, (uint64_t) low1, A.y);
+              int64_t xp_high = divcap(xp, (uint64_t) high, A.y);
+              int64_t l, min_hard;
+              if (A.gourdon) {
+                int64_t max_m = dmin(xpp, xp_low);
+                l = dpi(A.pitab, (uint64_t) max_m);
+                min_hard = dmax(xp_high, prime);
+              } else {
+                l = dpi(A.pitab, (uint64_t) dmin(xp_low, A.z / prime));
+                min_hard = dmax(xp_high, prime);
+              }
+              if (prime >= (int64_t) A.primes[l]) stop = true;
+              else {
+                P.lo = dpi(A.pitab, (uint64_t) dmin(min_hard, A.pi_max));
+                P.hi = l;
+                if (P.hi > P.lo) P.flags = 3;
+              }
+            }
+            if (stop) atomicMin(&s_stop, b);
+          }
+        }
+        lp[tid] = P;
+      }
+      __syncthreads();
+      const int bend = (int) dmin(b0 + NT - 1, Bs);
+      const int stop_at = s_stop;
+      for (int b = b0; b <= bend; b++) {
+        if (tid == 0) A.cnt[(int64_t) ws * cols + b] = total;
+        const LevelP P = lp[b - b0];
+        if ((P.flags & 1) && b < stop_at) {
+          if (dirty) { block_scan_chunks<NT>(ccount, pref, nch, wtmp); dirty = false; }
+          const uint64_t* xt = A.xp_tab + 3 * b;
+          const uint64_t xlo = xt[0], xhi = xt[1];
+          int smu_t = 0;
+          if (!(P.flags & 2)) {
+            const uint32_t thr = P.thr;
+            for (int64_t mi = P.hi - tid; mi > P.lo; mi -= NT) {
+              const uint32_t f = (uint32_t) factor[mi];
+              if (f > thr) {
+                const uint64_t m = 2310 * (uint64_t) (mi / 480) + cop[mi % 480];
+                const uint64_t n = div_xp(xlo, xhi, m);
+                const uint32_t c = query(bits, pref, (uint32_t) (n - (uint64_t) low));
+                const int sg = (f & 1) ? 1 : -1;
+                lsum += sg * (long long) c;
+                smu_t += sg;
+                nleaves++;
+              }
+            }
+            if (tid == 0) nentries += (unsigned long long) (P.hi - P.lo);
+          } else {
+            for (int64_t l = P.hi - tid; l > P.lo; l -= NT) {
+              const uint64_t q = A.primes[l];
+              const uint64_t n = div_xp(xlo, xhi, q);
+              const uint32_t c = query(bits, pref, (uint32_t) (n - (uint64_t) low));
+              lsum += c;
+              smu_t += 1;
+              nleaves++;
+              ntwo++;
+            }
+          }
+          for (int d = 16; d > 0; d >>= 1) smu_t += __shfl_down_sync(0xffffffffu, smu_t, d);
+          if (lane == 0 && smu_t) atomicAdd(&s_smu, smu_t);
+          __syncthreads();
+          if (tid == 0) { A.smu[(int64_t) ws * cols + b] = s_smu; s_smu = 0; }
+        }
+        // ---- cross off p_b and its multiples, count the bits removed first
+        if (P.jn) {
+          const uint64_t p = P.prime;
+          uint32_t rem = 0;
+          for (uint32_t j = tid; j < P.jn; j += NT) {
+            const uint64_t jj = P.jlo + j;
+            const uint64_t q = 30 * (jj >> 3) + woff((uint32_t) (jj & 7));
+            const uint32_t off = (uint32_t) (p * q - (uint64_t) low);
+            const uint32_t w = off / 240, r = off - w * 240;
+            const uint64_t m = 1ull << bit_of(r);
+            const uint64_t old = atomicAnd((unsigned long long*) &bits[w], ~m);
+            if (old & m) { rem++; atomicSub(&ccount[w >> 3], 1u); }
+          }
+          for (int d = 16; d > 0; d >>= 1) rem += __shfl_down_sync(0xffffffffu, rem, d);
+          if (lane == 0 && rem) atomicAdd(&s_rem[b % 3], rem);
+        }
+        __syncthreads();
+        const uint32_t r = s_rem[b % 3];
+        total -= r;
+        if (r) dirty = true;
+        if (tid == 0) s_rem[(b + 2) % 3] = 0;
+      }
+    }
+    // segment result
+    for (int d = 16; d > 0; d >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, d);
+    if (lane == 0) s_red[warp] = lsum;
+    for (int d = 16; d > 0; d >>= 1) {
+      nleaves += __shfl_down_sync(0xffffffffu, nleaves, d);
+      ntwo += __shfl_down_sync(0xffffffffu, ntwo, d);
+    }
+    if (lane == 0) {
+      if (nleaves) atomicAdd(&s_ctr[0], nleaves);
+      if (ntwo) atomicAdd(&s_ctr[1], ntwo);
+    }
+    if (tid == 0) { atomicAdd(&s_ctr[2], (unsigned long long) Bs); atomicAdd(&s_ctr[3], nentries); }
+    __syncthreads();
+    if (tid == 0) {
+      long long t = 0;
+      for (int i = 0; i < NT / 32; i++) t += s_red[i];
+      A.segsum[ws] = t;
+    }
+  }
+  __syncthreads();
+  if (tid < 4 && s_ctr[tid]) atomicAdd(&A.counters[tid], s_ctr[tid]);
+}
+
+// ---- phi offsets: acc[b] += sum_s M(s, b) * sum_{s'<s} C(s', b), in segment order
+__global__ void k_combine(const uint32_t* __restrict__ cnt, const int32_t* __restrict__ smu,
+                          int wave_len, int cols, int64_t* __restrict__ run, i128* __restrict__ acc)
+{
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= cols) return;
+  int64_t r = run[b];
+  i128 a = 0;
+  int s = 0;
+  for (; s + 4 <= wave_len; s += 4) {
+    int32_t m0 = smu[(int64_t) s * cols + b], m1 = smu[(int64_t) (s + 1) * cols + b];
+    int32_t m2 = smu[(int64_t) (s + 2) * cols + b], m3 = smu[(int64_t) (s + 3) * cols + b];
+    uint32_t c0 = cnt[(int64_t) s * cols + b], c1 = cnt[(int64_t) (s + 1) * cols + b];
+    uint32_t c2 = cnt[(int64_t) (s + 2) * cols + b], c3 = cnt[(int64_t) (s + 3) * cols + b];
+    a += (i128) m0 * r; r += c0;
+    a += (i128) m1 * r; r += c1;
+    a += (i128) m2 * r; r += c2;
+    a += (i128) m3 * r; r += c3;
+  }
+  for (; s < wave_len; s++) {
+    a += (i128) smu[(int64_t) s * cols + b] * r;
+    r += cnt[(int64_t) s * cols + b];
+  }
+  run[b] = r;
+  acc[b] += a;
+}
+
+// ---- local leaf sums of a wave into acc[0] (column 0 is never a level)
+__global__ void k_segsum(const int64_t* __restrict__ segsum, int n, i128* __restrict__ acc)
+{
+  __shared__ long long red[32];
+  i128 t = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) t += segsum[i];
+  // per-thread partial sums fit int64 (each segment's sum does, n is small)
+  long long v = (long long) t;
+  for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    i128 s = 0;
+    for (int i = 0; i < (int) (blockDim.x >> 5); i++) s += red[i];
+    acc[0] += s;
+  }
+}
+
+// ================================================================ host side
+static double now_ms()
+{
+  using namespace std::chrono;
+  return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+void DevBuf::alloc(size_t n)
+{
+  if (n <= bytes && p) return;
+  free_();
+  if (n == 0) n = 16;
+  cudaError_t e = cudaMalloc(&p, n);
+  if (e != cudaSuccess) {
+    p = nullptr;
+    bytes = 0;
+    cudaGetLastError();
+    fail(PCG_ENOMEM, std::string("cudaMalloc of ") + std::to_string(n) + " bytes failed: " + cudaGetErrorString(e));
+  }
+  bytes = n;
+}
+
+void DevBuf::free_()
+{
+  if (p) cudaFree(p);
+  p = nullptr;
+  bytes = 0;
+}
+
+DevBuf::~DevBuf() { free_(); }
+
+static std::vector<uint32_t> small_primes(int64_t limit)
+{
+  std::vector<uint8_t> c((size_t) limit + 1, 0);
+  std::vector<uint32_t> p;
+  for (int64_t i = 2; i <= limit; i++) {
+    if (c[i]) continue;
+    p.push_back((uint32_t) i);
+    for (int64_t m = i * i; m <= limit; m += i) c[m] = 1;
+  }
+  return p;
+}
+
+static void ensure_wheel(Ctx& c, cudaStream_t s)
+{
+  Tables& t = c.tab;
+  if (t.coprime.p) return;
+  const Wheel2310& w = wheel2310();
+  t.coprime.alloc(sizeof(w.coprime));
+  t.cindex.alloc(sizeof(w.index));
+  PCG_CUDA(cudaMemcpyAsync(t.coprime.p, w.coprime, sizeof(w.coprime), cudaMemcpyHostToDevice, s));
+  PCG_CUDA(cudaMemcpyAsync(t.cindex.p, w.index, sizeof(w.index), cudaMemcpyHostToDevice, s));
+}
+
+int64_t host_pi(const Tables& t, uint64_t x)
+{
+  static const int64_t tiny[6] = {0, 0, 1, 2, 2, 3};
+  if (x < 6) return tiny[x];
+  if ((int64_t) x > t.prime_limit) fail(PCG_EINTERNAL, "host_pi beyond the prime tables");
+  uint64_t i = x / 240;
+  uint64_t r = x % 240;
+  uint64_t m = 0;
+  for (int j = 0; j < 64; j++) {
+    static const int W[8] = {1, 7, 11, 13, 17, 19, 23, 29};
+    if ((uint64_t) (30 * (j / 8) + W[j % 8]) <= r) m |= 1ull << j;
+  }
+  return (int64_t) (t.h_pitab[2 * i] + (uint64_t) __builtin_popcountll(t.h_pitab[2 * i + 1] & m));
+}
+
+void ensure_prime_tables(Ctx& c, int64_t limit, cudaStream_t s)
+{
+  Tables& t = c.tab;
+  limit = std::max<int64_t>(limit, 240 * 4);
+  if (t.prime_limit >= limit) return;
+  ensure_wheel(c, s);
+  double t0 = now_ms();
+  int64_t nwords = limit / 240 + 1;
+  std::vector<uint32_t> base = small_primes(isqrt((u128) limit) + 1);
+  // base primes >= 7
+  std::vector<uint32_t> b7;
+  for (uint32_t p : base) if (p >= 7) b7.push_back(p);
+  DevBuf d_base, d_bits, d_pc, d_excl, d_sums;
+  d_base.alloc(std::max<size_t>(b7.size(), 1) * 4);
+  d_bits.alloc((size_t) nwords * 8);
+  d_pc.alloc((size_t) nwords * 4);
+  d_excl.alloc((size_t) nwords * 8);
+  int64_t nblk = (nwords + SCAN_ITEMS - 1) / SCAN_ITEMS;
+  d_sums.alloc((size_t) nblk * 8);
+  if (!b7.empty())
+    PCG_CUDA(cudaMemcpyAsync(d_base.p, b7.data(), b7.size() * 4, cudaMemcpyHostToDevice, s));
+  int64_t pblocks = (nwords + 2047) / 2048;
+  k_prime_bits<<<(unsigned) pblocks, 512, 2048 * 8, s>>>(d_bits.as<uint64_t>(), d_pc.as<uint32_t>(), nwords, limit,
+                                                         d_base.as<uint32_t>(), (int) b7.size());
+  PCG_CUDA(cudaGetLastError());
+  k_scan_sums<<<(unsigned) nblk, 512, 0, s>>>(d_pc.as<uint32_t>(), nwords, d_sums.as<uint64_t>());
+  k_scan_serial<<<1, 1024, 0, s>>>(d_sums.as<uint64_t>(), nblk);
+  k_scan_apply<<<(unsigned) nblk, 512, 0, s>>>(d_pc.as<uint32_t>(), nwords, d_sums.as<uint64_t>(), d_excl.as<uint64_t>());
+  PCG_CUDA(cudaGetLastError());
+  // total count -> nprimes
+  uint64_t last_excl = 0;
+  uint32_t last_pc = 0;
+  PCG_CUDA(cudaMemcpyAsync(&last_excl, d_excl.as<uint64_t>() + nwords - 1, 8, cudaMemcpyDeviceToHost, s));
+  PCG_CUDA(cudaMemcpyAsync(&last_pc, d_pc.as<uint32_t>() + nwords - 1, 4, cudaMemcpyDeviceToHost, s));
+  PCG_CUDA(cudaStreamSynchronize(s));
+  int64_t np = 3 + (int64_t) last_excl + last_pc;
+  t.primes.alloc((size_t) (np + 2) * 4);
+  t.pitab.alloc((size_t) nwords * 16);
+  uint32_t head[4] = {0, 2, 3, 5};
+  PCG_CUDA(cudaMemcpyAsync(t.primes.p, head, sizeof(head), cudaMemcpyHostToDevice, s));
+  k_pitab_primes<<<(unsigned) ((nwords + 255) / 256), 256, 0, s>>>(d_bits.as<uint64_t>(), d_excl.as<uint64_t>(), nwords,
+                                                                   t.pitab.as<uint64_t>(), t.primes.as<uint32_t>());
+  PCG_CUDA(cudaGetLastError());
+  t.h_pitab.resize((size_t) nwords * 2);
+  PCG_CUDA(cudaMemcpyAsync(t.h_pitab.data(), t.pitab.p, (size_t) nwords * 16, cudaMemcpyDeviceToHost, s));
+  t.h_primes.resize((size_t) np + 1);
+  PCG_CUDA(cudaMemcpyAsync(t.h_primes.data(), t.primes.p, ((size_t) np + 1) * 4, cudaMemcpyDeviceToHost, s));
+  PCG_CUDA(cudaStreamSynchronize(s));
+  t.prime_limit = limit;
+  t.nprimes = np;
+  t.build_ms += now_ms() - t0;
+}
+
+template <typename T>
+static void build_factor(Ctx& c, DevBuf& out, int64_t limit, int64_t y, int gourdon, cudaStream_t s)
+{
+  Tables& t = c.tab;
+  const Wheel2310& w = wheel2310();
+  int64_t size = w.to_index((uint64_t) std::max<int64_t>(limit, 1)) + 1;
+  out.alloc((size_t) size * sizeof(T));
+  int64_t sq = isqrt((u128) limit);
+  int64_t nsmall = host_pi(t, (uint64_t) sq);
+  int64_t blocks = (size + FT_E - 1) / FT_E;
+  size_t smem = FT_E * (8 + 4 + 4) + 480 * 2 + 2310 * 2;
+  PCG_CUDA(cudaFuncSetAttribute(k_factor<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+  k_factor<T><<<(unsigned) blocks, 512, smem, s>>>(out.as<T>(), size, limit, y, gourdon, t.primes.as<uint32_t>(),
+                                                   nsmall, t.coprime.as<uint16_t>(), t.cindex.as<int16_t>());
+  PCG_CUDA(cudaGetLastError());
+  if (gourdon && sq > y) {
+    // small primes in (y, sqrt(limit)]: their multiples have a prime factor > y
+    int64_t kf = host_pi(t, (uint64_t) y) + 1;
+    kf = std::max<int64_t>(kf, 6);
+    if (kf <= nsmall)
+      k_factor_zero_small<T><<<(unsigned) (nsmall - kf + 1), 256, 0, s>>>(out.as<T>(), size, limit, t.primes.as<uint32_t>(),
+                                                                           kf, nsmall, t.coprime.as<uint16_t>(),
+                                                                           t.cindex.as<int16_t>());
+    PCG_CUDA(cudaGetLastError());
+  }
+}
+
+void ensure_factor_d(Ctx& c, int64_t y, int64_t z, cudaStream_t s)
+{
+  Tables& t = c.tab;
+  bool ok = t.fd_z >= z && (t.fd_y == y || (y >= z && t.fd_y >= z));
+  if (ok) return;
+  if (z > 386083ll * 386083 - 1 && false) fail(PCG_ERANGE, "z too large");
+  double t0 = now_ms();
+  ensure_prime_tables(c, std::max<int64_t>(y, isqrt((u128) z) + 1), s);
+  t.fd_bytes = (z <= 386083ll * 386083 - 1) ? 2 : 4;
+  if (t.fd_bytes == 2) build_factor<uint16_t>(c, t.factor_d, z, y, 1, s);
+  else build_factor<uint32_t>(c, t.factor_d, z, y, 1, s);
+  PCG_CUDA(cudaStreamSynchronize(s));
+  t.fd_y = y;
+  t.fd_z = z;
+  t.build_ms += now_ms() - t0;
+}
+
+void ensure_factor_dr(Ctx& c, int64_t y, cudaStream_t s)
+{
+  Tables& t = c.tab;
+  if (t.fr_y >= y) return;
+  double t0 = now_ms();
+  ensure_prime_tables(c, std::max<int64_t>(y, isqrt((u128) y) + 1), s);
+  t.fr_bytes = (y <= 65534ll * 65534 - 1) ? 2 : 4;
+  if (t.fr_bytes == 2) build_factor<uint16_t>(c, t.factor_dr, y, y, 0, s);
+  else build_factor<uint32_t>(c, t.factor_dr, y, y, 0, s);
+  PCG_CUDA(cudaStreamSynchronize(s));
+  t.fr_y = y;
+  t.build_ms += now_ms() - t0;
+}
+
+template <typename FT, int NT>
+static void launch_sweep(const SweepArgs& a, int grid, size_t smem, cudaStream_t s)
+{
+  static bool attr_set = false;
+  if (!attr_set) {
+    PCG_CUDA(cudaFuncSetAttribute(k_sweep<FT, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr_set = true;
+  }
+  k_sweep<FT, NT><<<grid, NT, smem, s>>>(a);
+}
+
+SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaStream_t s)
+{
+  SweepResult res;
+  pcg_stats& st = res.stats;
+  double t_start = now_ms();
+  c.tab.build_ms = 0;
+  const u128 x = pb.x;
+  int64_t L, x_star = 0, pi_sqrt, bglob;
+  int64_t pi_limit;
+  if (pb.gourdon) {
+    L = (int64_t) (x / (u128) pb.z);
+    x_star = x_star_gourdon(x, pb.y);
+    pi_limit = pb.y;
+    ensure_prime_tables(c, pi_limit, s);
+    ensure_factor_d(c, pb.y, pb.z, s);
+    pi_sqrt = host_pi(c.tab, (uint64_t) isqrt((u128) pb.z));
+    bglob = host_pi(c.tab, (uint64_t) x_star);
+  } else {
+    L = pb.z;
+    int64_t max_prime = std::min<int64_t>(pb.y, pb.z / std::max<int64_t>(isqrt((u128) pb.y), 1));
+    pi_limit = std::max<int64_t>(pb.y, max_prime);
+    ensure_prime_tables(c, pi_limit, s);
+    ensure_factor_dr(c, pb.y, s);
+    pi_sqrt = host_pi(c.tab, (uint64_t) isqrt((u128) pb.y));
+    bglob = std::max<int64_t>(pi_sqrt, host_pi(c.tab, (uint64_t) std::min<int64_t>(isqrt((u128) pb.z), pb.y)));
+    bglob = std::min<int64_t>(bglob, host_pi(c.tab, (uint64_t) max_prime));
+  }
+  st.table_ms = c.tab.build_ms;
+  if (L <= 0 || bglob < 1) {
+    st.total_ms = now_ms() - t_start;
+    return res;
+  }
+  const int cols = (int) bglob + 1;
+
+  // x / p_b and x / p_b^3 per level
+  std::vector<uint64_t> xp((size_t) cols * 3, 0);
+  for (int64_t b = 1; b <= bglob; b++) {
+    u128 p = c.tab.h_primes[(size_t) b];
+    u128 q = x / p;
+    u128 q3 = q / (p * p);
+    xp[3 * b] = (uint64_t) q;
+    xp[3 * b + 1] = (uint64_t) (q >> 64);
+    xp[3 * b + 2] = q3 > (u128) INT64_MAX ? (uint64_t) INT64_MAX : (uint64_t) q3;
+  }
+
+  // tuning
+  int words = tune.segment_words > 0 ? tune.segment_words : 8192;
+  const int NT = 512;
+  words = std::max(words, 8 * NT);
+  words = (words + 8 * NT - 1) / (8 * NT) * (8 * NT);
+  int ctas = tune.ctas_per_sm > 0 ? tune.ctas_per_sm : 2;
+  int64_t seg = (int64_t) words * 240;
+  int64_t nseg = (L + seg - 1) / seg;
+  int grid = c.num_sms * ctas;
+  size_t smem = (size_t) words * 8 + (size_t) (words / 8) * 8 + sizeof(LevelP) * NT + 480 * 2 + 16;
+  if (smem > 200 * 1024) fail(PCG_EINVAL, "segment too large for shared memory");
+  int64_t wave_cap = (int64_t) grid * 8;
+  // budget of the C/M matrices: 1 GiB
+  int64_t max_rows = std::max<int64_t>(1, (int64_t) (1ull << 30) / ((int64_t) cols * 8));
+  int64_t wave_len = std::min<int64_t>({nseg, wave_cap, max_rows});
+
+  c.cnt.alloc((size_t) wave_len * cols * 4);
+  c.smu.alloc((size_t) wave_len * cols * 4);
+  c.segsum.alloc((size_t) wave_len * 8);
+  c.run.alloc((size_t) cols * 8);
+  c.acc.alloc((size_t) cols * 16);
+  c.misc.alloc(4096);
+  uint64_t* d_xp = nullptr;
+  DevBuf xpbuf;
+  xpbuf.alloc(xp.size() * 8);
+  d_xp = xpbuf.as<uint64_t>();
+  PCG_CUDA(cudaMemcpyAsync(d_xp, xp.data(), xp.size() * 8, cudaMemcpyHostToDevice, s));
+  PCG_CUDA(cudaMemsetAsync(c.run.p, 0, (size_t) cols * 8, s));
+  PCG_CUDA(cudaMemsetAsync(c.acc.p, 0, (size_t) cols * 16, s));
+  PCG_CUDA(cudaMemsetAsync(c.misc.p, 0, 4096, s));
+  unsigned long long* d_counters = (unsigned long long*) c.misc.p;
+  int* d_queue = (int*) ((char*) c.misc.p + 64);
+
+  SweepArgs a;
+  memset(&a, 0, sizeof(a));
+  a.x_lo = (uint64_t) x;
+  a.x_hi = (uint64_t) (x >> 64);
+  a.y = pb.y;
+  a.z = pb.z;
+  a.k = pb.k;
+  a.L = L;
+  a.x_star = x_star;
+  a.seg = seg;
+  a.words = words;
+  a.gourdon = pb.gourdon;
+  a.pi_sqrt = (int) pi_sqrt;
+  a.bglob = (int) bglob;
+  a.primes = c.tab.primes.as<uint32_t>();
+  a.nprimes = c.tab.nprimes;
+  a.pitab = c.tab.pitab.as<uint64_t>();
+  a.pi_max = c.tab.prime_limit;
+  a.factor = pb.gourdon ? c.tab.factor_d.p : c.tab.factor_dr.p;
+  int fbytes = pb.gourdon ? c.tab.fd_bytes : c.tab.fr_bytes;
+  a.xp_tab = d_xp;
+  a.coprime = c.tab.coprime.as<uint16_t>();
+  a.cindex = c.tab.cindex.as<int16_t>();
+  a.cnt = c.cnt.as<uint32_t>();
+  a.smu = c.smu.as<int32_t>();
+  a.segsum = c.segsum.as<int64_t>();
+  a.counters = d_counters;
+
+  PCG_CUDA(cudaEventRecord(c.ev[0], s));
+  uint64_t launches = 0;
+  float ms_sweep = 0, ms_comb = 0;
+  int waves = 0;
+  for (int64_t first = 0; first < nseg; first += wave_len) {
+    int wl = (int) std::min<int64_t>(wave_len, nseg - first);
+    a.wave_first = first;
+    a.wave_len = wl;
+    a.queue = d_queue + (waves % 16);
+    PCG_CUDA(cudaMemsetAsync(c.cnt.p, 0, (size_t) wl * cols * 4, s));
+    PCG_CUDA(cudaMemsetAsync(c.smu.p, 0, (size_t) wl * cols * 4, s));
+    if (waves % 16 == 0 && waves > 0) PCG_CUDA(cudaMemsetAsync(d_queue, 0, 64, s));
+    int g = (int) std::min<int64_t>(grid, wl);
+    if (fbytes == 2) launch_sweep<uint16_t, 512>(a, g, smem, s);
+    else launch_sweep<uint32_t, 512>(a, g, smem, s);
+    PCG_CUDA(cudaGetLastError());
+    k_combine<<<(cols + 255) / 256, 256, 0, s>>>(a.cnt, a.smu, wl, cols, c.run.as<int64_t>(), c.acc.as<i128>());
+    k_segsum<<<1, 1024, 0, s>>>(a.segsum, wl, c.acc.as<i128>());
+    PCG_CUDA(cudaGetLastError());
+    launches += 3;
+    waves++;
+  }
+  PCG_CUDA(cudaEventRecord(c.ev[1], s));
+  std::vector<i128> acc((size_t) cols);
+  unsigned long long ctr[4];
+  PCG_CUDA(cudaMemcpyAsync(acc.data(), c.acc.p, (size_t) cols * 16, cudaMemcpyDeviceToHost, s));
+  PCG_CUDA(cudaMemcpyAsync(ctr, d_counters, sizeof(ctr), cudaMemcpyDeviceToHost, s));
+  PCG_CUDA(cudaStreamSynchronize(s));
+  PCG_CUDA(cudaEventElapsedTime(&ms_sweep, c.ev[0], c.ev[1]));
+  i128 sum = 0;
+  for (int b = 0; b < cols; b++) sum += acc[(size_t) b];
+  res.sum = sum;
+  st.leaves = ctr[0];
+  st.two_prime_leaves = ctr[1];
+  st.levels = ctr[2];
+  st.factor_entries = ctr[3];
+  st.segments = (uint64_t) nseg;
+  st.kernel_launches = launches;
+  st.sweep_ms = ms_sweep;
+  st.combine_ms = ms_comb;
+  st.segment_words = words;
+  st.ctas_per_sm = ctas;
+  st.threads_per_cta = NT;
+  st.total_ms = now_ms() - t_start;
+  return res;
+}
+
+}  // namespace pcg
