@@ -1,0 +1,272 @@
+#!/usr/bin/env python3
+"""Headline benchmark: Gourdon's D(1e20) (the hard special leaves of
+pi(1e20)) on one GB300, in hard-leaves/s.
+
+One step = one D(x, y, z, k) evaluation at x = 1e20 with the reference's
+default parameters (y = z = 245535363, k = 8): the full sieve of [0, x/z)
+and all 22 178 370 075 hard leaves.
+
+value        device-timed (CUDA events on the launching stream), tables
+             resident in HBM, L2 flushed between steps.
+e2e          the C-ABI call pcg_D on a fresh context: table construction,
+             host->device parameter copies, the sweep and the device->host
+             result copy, host wall clock.
+roofline     the sieve/leaf kernel (k_sweep): algorithmic table bytes
+             (2 B per FactorTable entry read, 4 B per two-prime leaf,
+             16 B per (segment, b) PiTable/level step) over its launch time.
+cpu_baseline the oracle's restatement of the reference's chunk loop on this
+             host's cores, timed on an evenly spread sample of the same
+             interval and scaled to the whole interval.
+
+--impl reference: the CPU reference arm (the oracle port, all host threads).
+--gpus N > 1: replicas only -- each rank evaluates its own D(1e20).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+X = 10 ** 20
+WORKLOAD = "D(1e20) hard special leaves, Gourdon default parameters (y=z=245535363, k=8)"
+METRIC = "D(1e20) hard-leaves/s on 1 GB300"
+UNIT = "hard-leaves/s"
+TOTAL_LEAVES_1E20 = 22178370075
+
+
+def clocks_sampler(stop, out):
+    cmd = ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+           "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+           "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+           "--format=csv,noheader,nounits", "-lms", "200"]
+    try:
+        p = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+    except Exception:
+        return
+    while not stop.is_set():
+        line = p.stdout.readline()
+        if not line:
+            break
+        out.append(line.strip())
+    p.terminate()
+
+
+def summarize_clocks(rows, dev):
+    sm, mx, reasons = [], 0, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for r in rows:
+        f = [t.strip() for t in r.split(",")]
+        if len(f) < 9 or f[0] != str(dev):
+            continue
+        try:
+            sm.append(float(f[1]))
+            mx = max(mx, float(f[2]))
+        except ValueError:
+            continue
+        for n, v in zip(names, f[5:9]):
+            if v.lower().startswith("active"):
+                reasons.add(n)
+    sm.sort()
+    return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx or None,
+            "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs"), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per full D(1e20) from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "k_sweep_traffic.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p))
+        except Exception:
+            return None
+    return None
+
+
+def cpu_baseline(p, threads, target_s=12.0):
+    """Oracle restatement of the reference's chunk loop on a spread sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.load()
+    nchunks = max(64, 4 * threads)
+    frac = 2e-4
+    leaves, secs = oracle.D_sample(X, p["y"], p["z"], p["k"], nchunks, frac, threads)
+    if secs > 0 and secs < target_s / 4:
+        frac = min(0.05, frac * target_s / max(secs, 1e-3))
+        leaves, secs = oracle.D_sample(X, p["y"], p["z"], p["k"], nchunks, frac, threads)
+    est_total_s = secs / frac
+    return {"value": TOTAL_LEAVES_1E20 / est_total_s, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "oracle chunk loop over %d evenly spread chunks = %.4g of [0, x/z) of D(1e20), "
+                      "%.1f s wall, %d leaves; scaled to the whole interval (est. %.0f s for D(1e20))"
+                      % (nchunks, frac, secs, leaves, est_total_s),
+            "sample_seconds": secs, "est_total_seconds": est_total_s}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    import primecount_gb300 as pcg
+    p = pcg.gourdon_params(X)
+    threads = os.cpu_count() or 1
+    vals = []
+    for _ in range(args.warmup):
+        pass
+    t0 = time.time()
+    for _ in range(args.steps):
+        cb = cpu_baseline(p, threads, target_s=8.0)
+        vals.append(cb["value"])
+    dt = time.time() - t0
+    v = sum(vals) / len(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64/int128",
+            "data": "synthetic (scalar x)", "config": {"workload": WORKLOAD, "x": "1e20", "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": cb["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--x", default="1e20", help="smaller x for profiling runs (the headline is 1e20)")
+    args = ap.parse_args()
+    global X
+    X = int(float(args.x)) if "e" in args.x else int(args.x)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import torch
+    import primecount_gb300 as pcg
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    p = pcg.gourdon_params(X)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    ctx = pcg.Context(0)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def step():
+        return pcg.D(X, p["y"], p["z"], p["k"], ctx=ctx, stream=sptr)
+
+    for _ in range(max(args.warmup, 1)):
+        v = step()
+    stats0 = ctx.last_stats()
+
+    rows = []
+    stop = threading.Event()
+    th = threading.Thread(target=clocks_sampler, args=(stop, rows), daemon=True)
+    th.start()
+    time.sleep(0.5)
+
+    barrier()
+    torch.cuda.synchronize()
+    evs = []
+    kernel_ms = 0.0
+    launches = 0
+    t0 = time.time()
+    for i in range(args.steps):
+        flush.fill_(i & 0xFF)
+        s_ev = torch.cuda.Event(enable_timing=True)
+        e_ev = torch.cuda.Event(enable_timing=True)
+        s_ev.record(stream)
+        v = step()
+        e_ev.record(stream)
+        evs.append((s_ev, e_ev))
+        st = ctx.last_stats()
+        kernel_ms += st["sweep_kernel_ms"]
+        launches += st["sweep_launches"]
+    torch.cuda.synchronize()
+    barrier()
+    wall = time.time() - t0
+    stop.set()
+    th.join(timeout=2)
+    dev_ms = [a.elapsed_time(b) for a, b in evs]
+    ms_step = sum(dev_ms) / len(dev_ms)
+    if dist is not None:
+        t = torch.tensor([ms_step], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    leaves = st["leaves"]
+    value = world * leaves / (ms_step / 1000.0)
+
+    # e2e: the C-ABI call on a fresh context (tables built inside the call)
+    e2e_t, h2d, d2h = [], 0, 0
+    for _ in range(args.e2e_steps):
+        c2 = pcg.Context(0)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        v2 = pcg.D(X, p["y"], p["z"], p["k"], ctx=c2)
+        e2e_t.append(time.perf_counter() - t1)
+        s2 = c2.last_stats()
+        h2d, d2h = s2["h2d_bytes"], s2["d2h_bytes"]
+        c2.close()
+        assert v2 == v
+    e2e_s = sum(e2e_t) / len(e2e_t) if e2e_t else float("nan")
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peaks()
+    alg_bytes = 2 * st["factor_entries"] + 4 * st["two_prime_leaves"] + 16 * st["levels"]
+    k_ms_call = kernel_ms / args.steps
+    launches_call = launches / args.steps
+    achieved = alg_bytes / (k_ms_call / 1000.0) / 1e9
+    tr = profile_traffic()
+    traffic = tr["dram_bytes_per_launch"] if tr else None
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+            "kernel": "k_sweep", "alg_bytes_per_launch": alg_bytes / launches_call,
+            "launch_ms": k_ms_call / launches_call, "launches_per_step": launches_call}
+    cpu = None
+    if not args.no_cpu and X == 10 ** 20:
+        cpu = cpu_baseline(p, os.cpu_count() or 1)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int64/int128", "data": "synthetic (scalar x)",
+            "config": {"workload": WORKLOAD if X == 10 ** 20 else "D(%s)" % args.x, "x": args.x, "y": p["y"], "z": p["z"], "k": p["k"],
+                       "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas" if world > 1 else "1 GPU",
+                       "segment_words": st["segment_words"], "ctas_per_sm": st["ctas_per_sm"]},
+            "result": str(v), "leaves_per_step": leaves,
+            "e2e": {"value": leaves / e2e_s, "unit": UNIT, "seconds": e2e_s,
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(st["kernel_launches"]) * args.steps,
+            "roofline": roof, "cpu_baseline": cpu,
+            "clocks": summarize_clocks(rows, torch.cuda.current_device()),
+            "wall_s": wall}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -67,6 +67,7 @@ typedef struct {
   int print;             /* reference is_print: print variables and timings            */
   int segment_words;     /* sieve segment in 64-bit words (x240 numbers); 0 = autotune */
   int ctas_per_sm;       /* resident CTAs per SM for the sweep; 0 = autotune           */
+  int cta_threads;       /* threads per sweep CTA: 128, 256 or 512; 0 = autotune       */
 } pcg_opts;
 
 /* Work and time of the last call on a context. */
@@ -81,6 +82,10 @@ typedef struct {
   double sweep_ms;         /* sieve + leaf kernels                                    */
   double combine_ms;       /* phi-offset scan and reduction                           */
   double total_ms;         /* whole call, host clock                                  */
+  double sweep_kernel_ms;  /* sum of the sieve/leaf kernel launches (CUDA events)     */
+  uint64_t sweep_launches; /* launches of the sieve/leaf kernel                       */
+  uint64_t h2d_bytes;      /* host -> device bytes copied by the call                 */
+  uint64_t d2h_bytes;      /* device -> host bytes copied by the call                 */
   int segment_words;       /* tuning actually used                                    */
   int ctas_per_sm;
   int threads_per_cta;

@@ -40,6 +40,9 @@ def load():
             fn.argtypes = [u64, i64, i64, i64, i64, ctypes.c_int, ctypes.POINTER(u64), ctypes.POINTER(i64),
                            ctypes.POINTER(Stats)]
             fn.restype = ctypes.c_int
+        L.ora_D_sample.argtypes = [u64, i64, i64, i64, i64, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                   ctypes.POINTER(i64), ctypes.POINTER(ctypes.c_double)]
+        L.ora_D_sample.restype = ctypes.c_int
         L.ora_phi.argtypes = [i64, i64]
         L.ora_phi.restype = i64
         L.ora_pi_sieve.argtypes = [i64]
@@ -74,6 +77,14 @@ def D(x, y, z, k, threads=1):
 def S2_hard(x, y, z, c, threads=1):
     """(S2_hard(x, y, z, c), work counters) -- restatement of S2_hard.cpp."""
     return _hard(load().ora_S2_hard, x, y, z, c, threads)
+
+
+def D_sample(x, y, z, k, nchunks, fraction, threads):
+    """(leaves, seconds) of the reference's chunk loop on a sample of D's interval."""
+    leaves, secs = ctypes.c_int64(), ctypes.c_double()
+    load().ora_D_sample(x & 0xFFFFFFFFFFFFFFFF, x >> 64, y, z, k, nchunks, fraction, threads,
+                        ctypes.byref(leaves), ctypes.byref(secs))
+    return leaves.value, secs.value
 
 
 def phi(x, a):

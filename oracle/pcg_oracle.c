@@ -697,6 +697,69 @@ static i128 sweep_run(sweep* w, int threads, ora_stats* st)
   return total;
 }
 
+/* CPU-baseline sample: run the reference's chunk loop (sweep_chunk) over
+ * `nchunks` sub-intervals spread evenly over [0, x/z), together `fraction`
+ * of the interval, in parallel.  phi offsets are zero (they do not change the
+ * work); the leaves evaluated and the wall time are returned. */
+int ora_D_sample(uint64_t x_lo, int64_t x_hi, int64_t y, int64_t z, int64_t k,
+                 int nchunks, double fraction, int threads, int64_t* leaves, double* seconds)
+{
+  init_tables();
+  u128 x = make_u128(x_lo, x_hi);
+  sweep w;
+  memset(&w, 0, sizeof(w));
+  w.gourdon = 1;
+  w.x = x;
+  w.y = y;
+  w.z = z;
+  w.k = k;
+  w.limit = (int64_t) (x / (u128) z);
+  w.x_star = x_star_gourdon(x, y);
+  pitable pt;
+  pitable_build(&pt, y);
+  w.pi = &pt;
+  w.pi_sqrt = pit(&pt, (uint64_t) isqrt64(z));
+  int64_t np;
+  int64_t* primes = primes_upto(y, &np);
+  w.primes = primes;
+  w.nprimes = np;
+  int64_t fsz = ora_factor_size(z);
+  uint32_t* factor = (uint32_t*) malloc(sizeof(uint32_t) * (size_t) fsz);
+  factor_build(1, y, z, 0xFFFF, factor);
+  w.factor = factor;
+  int64_t seg = 1 << 20;
+  seg = (seg / 240 + 1) * 240;
+  int64_t span = (int64_t) ((double) w.limit * fraction / nchunks);
+  span = (span / seg + 1) * seg;
+  int64_t total = 0;
+  double t0 = 0;
+#ifdef _OPENMP
+  t0 = omp_get_wtime();
+#endif
+  #pragma omp parallel for schedule(dynamic, 1) num_threads(threads) reduction(+:total)
+  for (int c = 0; c < nchunks; c++) {
+    int64_t lo = (int64_t) ((double) w.limit * c / nchunks);
+    lo -= lo % seg;
+    int64_t hi = lo + span < w.limit ? lo + span : w.limit;
+    int64_t* phi = (int64_t*) calloc((size_t) (np + 2), sizeof(int64_t));
+    ora_stats st;
+    memset(&st, 0, sizeof(st));
+    for (int64_t a = lo; a < hi; a += seg) sweep_chunk(&w, a, a + seg < hi ? a + seg : hi, seg, phi, &st);
+    total += st.leaves;
+    free(phi);
+  }
+#ifdef _OPENMP
+  *seconds = omp_get_wtime() - t0;
+#else
+  *seconds = 0;
+#endif
+  *leaves = total;
+  free(factor);
+  free(primes);
+  free(pt.t);
+  return 0;
+}
+
 static void split128(i128 v, uint64_t* lo, int64_t* hi)
 {
   *lo = (uint64_t) v;

@@ -46,6 +46,12 @@ int ora_D(uint64_t x_lo, int64_t x_hi, int64_t y, int64_t z, int64_t k,
 int ora_S2_hard(uint64_t x_lo, int64_t x_hi, int64_t y, int64_t z, int64_t c,
                 int threads, uint64_t* out_lo, int64_t* out_hi, ora_stats* stats);
 
+/* CPU baseline: leaves evaluated and wall seconds of the reference's chunk
+ * loop over `nchunks` evenly spread sub-intervals (together `fraction` of
+ * [0, x/z)), run on `threads` threads. */
+int ora_D_sample(uint64_t x_lo, int64_t x_hi, int64_t y, int64_t z, int64_t k,
+                 int nchunks, double fraction, int threads, int64_t* leaves, double* seconds);
+
 /* Partial sieve function phi(x, a) by Legendre's recurrence with a small
  * cache (reference semantics: src/phi.cpp:410-430).  Small inputs only. */
 int64_t ora_phi(int64_t x, int64_t a);

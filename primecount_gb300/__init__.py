@@ -39,7 +39,8 @@ class I128(ctypes.Structure):
 
 class Opts(ctypes.Structure):
     _fields_ = [("ctx", ctypes.c_void_p), ("stream", ctypes.c_void_p), ("threads", ctypes.c_int),
-                ("print", ctypes.c_int), ("segment_words", ctypes.c_int), ("ctas_per_sm", ctypes.c_int)]
+                ("print", ctypes.c_int), ("segment_words", ctypes.c_int), ("ctas_per_sm", ctypes.c_int),
+                ("cta_threads", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -48,6 +49,8 @@ class Stats(ctypes.Structure):
                 ("factor_entries", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
                 ("table_ms", ctypes.c_double), ("sweep_ms", ctypes.c_double),
                 ("combine_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
+                ("sweep_kernel_ms", ctypes.c_double), ("sweep_launches", ctypes.c_uint64),
+                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
                 ("segment_words", ctypes.c_int), ("ctas_per_sm", ctypes.c_int),
                 ("threads_per_cta", ctypes.c_int)]
 
@@ -149,7 +152,7 @@ class Context:
         return s.as_dict()
 
 
-def _opts(ctx=None, stream=None, threads=0, print_=False, segment_words=0, ctas_per_sm=0):
+def _opts(ctx=None, stream=None, threads=0, print_=False, segment_words=0, ctas_per_sm=0, cta_threads=0):
     o = Opts()
     o.ctx = ctx._h if ctx is not None else None
     o.stream = stream
@@ -157,6 +160,7 @@ def _opts(ctx=None, stream=None, threads=0, print_=False, segment_words=0, ctas_
     o.print = 1 if print_ else 0
     o.segment_words = segment_words
     o.ctas_per_sm = ctas_per_sm
+    o.cta_threads = cta_threads
     return o
 
 
@@ -166,18 +170,19 @@ def last_stats(ctx=None):
     return s.as_dict()
 
 
-def D(x, y, z, k, threads=0, print=False, ctx=None, stream=None, segment_words=0, ctas_per_sm=0):
+def D(x, y, z, k, threads=0, print=False, ctx=None, stream=None, segment_words=0, ctas_per_sm=0, cta_threads=0):
     """Gourdon's D(x, y, z, k): the hard special leaves (src/gourdon/D.cpp)."""
     out = I128()
-    o = _opts(ctx, stream, threads, print, segment_words, ctas_per_sm)
+    o = _opts(ctx, stream, threads, print, segment_words, ctas_per_sm, cta_threads)
     _check(load().pcg_D(to_i128(x), int(y), int(z), int(k), ctypes.byref(o), ctypes.byref(out)), ctx)
     return from_i128(out)
 
 
-def S2_hard(x, y, z, c, threads=0, print=False, ctx=None, stream=None, segment_words=0, ctas_per_sm=0):
+def S2_hard(x, y, z, c, threads=0, print=False, ctx=None, stream=None, segment_words=0, ctas_per_sm=0,
+            cta_threads=0):
     """Deleglise-Rivat's S2_hard(x, y, z, c) (src/deleglise-rivat/S2_hard.cpp)."""
     out = I128()
-    o = _opts(ctx, stream, threads, print, segment_words, ctas_per_sm)
+    o = _opts(ctx, stream, threads, print, segment_words, ctas_per_sm, cta_threads)
     _check(load().pcg_S2_hard(to_i128(x), int(y), int(z), int(c), ctypes.byref(o), ctypes.byref(out)), ctx)
     return from_i128(out)
 

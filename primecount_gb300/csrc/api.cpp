@@ -169,6 +169,7 @@ DrParams dr_params(u128 x)
 Ctx::~Ctx()
 {
   for (auto& e : ev) if (e) cudaEventDestroy(e);
+  for (auto& e : kev) if (e) cudaEventDestroy(e);
   if (own_stream && stream) cudaStreamDestroy(stream);
 }
 
@@ -245,6 +246,7 @@ static Tuning tuning_from(const pcg_opts* o)
   if (o) {
     t.segment_words = o->segment_words;
     t.ctas_per_sm = o->ctas_per_sm;
+    t.cta_threads = o->cta_threads;
   }
   return t;
 }

@@ -110,6 +110,7 @@ struct SweepProblem {
 struct Tuning {
   int segment_words = 0;
   int ctas_per_sm = 0;
+  int cta_threads = 0;
 };
 
 struct SweepResult {
@@ -133,6 +134,7 @@ struct Ctx {
   pcg_stats last{};
   std::string last_error;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  std::vector<cudaEvent_t> kev;   // per-launch timing events of the sweep
   ~Ctx();
 };
 

@@ -92,7 +92,15 @@ __device__ int64_t disqrt(u128 x)
 __device__ __forceinline__ int64_t divcap(u128 a, uint64_t d, int64_t cap)
 {
   if ((u128) d * (u128) cap <= a) return cap;
+  if ((uint64_t) (a >> 64) == 0) return (int64_t) ((uint64_t) a / d);
   return (int64_t) (a / d);
+}
+
+// a / d for a 128-bit a, 64-bit division when the high word is zero
+__device__ __forceinline__ u128 div128(u128 a, uint64_t d)
+{
+  if ((uint64_t) (a >> 64) == 0) return (u128) ((uint64_t) a / d);
+  return a / d;
 }
 
 // ================================================================ prime tables
@@ -353,14 +361,17 @@ struct LevelP {
   uint32_t jn;        // number of cross-off co-factors
   uint32_t prime;
   uint32_t thr;       // factor-table threshold (family 1)
-  uint32_t flags;     // 1: leaves, 2: family 2
+  uint32_t flags;     // 1: leaves, 2: family 2, 4: small prime (pattern cross-off), 8: formula count
+  int32_t level;      // b
+  uint32_t fcount;    // flag 8: numbers of the segment removed at this level (PiTable formula)
 };
 
 struct SweepArgs {
   uint64_t x_lo, x_hi;
   int64_t y, z, k, L, x_star;
-  int64_t seg;           // numbers per segment = words * 240
-  int32_t words;
+  const int64_t* seglo;  // segment s = [seglo[s], seglo[s+1])
+  int32_t words;         // bitmap words per CTA (max segment = words * 240 numbers)
+  int32_t rec_cap;       // leaf records per chunk
   int32_t gourdon;
   int32_t pi_sqrt;       // last level of family 1
   int32_t bglob;         // columns = bglob + 1
@@ -381,6 +392,11 @@ struct SweepArgs {
   unsigned long long* counters;  // [0] leaves, [1] two-prime leaves, [2] levels, [3] factor entries
   int* queue;
 };
+
+// primes 7..61 sieved with wheel patterns (their multiples repeat every p words)
+#define NSMALL 15
+#define PAT_WORDS 491   // 7+11+13+17+19+23+29+31+37+41+43+47+53+59+61
+__constant__ uint32_t c_small_p[NSMALL + 1] = {7, 11, 13, 17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61, 0};
 
 // x / m for m < 2^32 when the quotient is known to fit in 63 bits
 __device__ __forceinline__ uint64_t div_xp32(uint64_t xlo, uint64_t xhi, uint32_t m)
@@ -404,9 +420,10 @@ template <int NT>
 __device__ __forceinline__ void block_scan_chunks(const uint32_t* __restrict__ ccount, uint32_t* __restrict__ pref,
                                                   int nch, uint32_t* wtmp)
 {
+  // exclusive prefix of the chunk counts; two barriers: warp totals, then the result
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int cpt = nch / NT;      // nch is a multiple of NT
-  int base = tid * cpt;
+  const int base = tid * cpt;
   uint32_t s = 0;
   for (int c = 0; c < cpt; c++) s += ccount[base + c];
   uint32_t incl = s;
@@ -416,16 +433,8 @@ __device__ __forceinline__ void block_scan_chunks(const uint32_t* __restrict__ c
   }
   if (lane == 31) wtmp[warp] = incl;
   __syncthreads();
-  if (warp == 0) {
-    uint32_t a = lane < NT / 32 ? wtmp[lane] : 0, ai = a;
-    for (int d = 1; d < 32; d <<= 1) {
-      uint32_t t = __shfl_up_sync(0xffffffffu, ai, d);
-      if (lane >= d) ai += t;
-    }
-    if (lane < NT / 32) wtmp[lane] = ai - a;
-  }
-  __syncthreads();
-  uint32_t run = wtmp[warp] + incl - s;
+  uint32_t run = incl - s;
+  for (int w = 0; w < warp; w++) run += wtmp[w];
   for (int c = 0; c < cpt; c++) {
     pref[base + c] = run;
     run += ccount[base + c];
@@ -437,24 +446,70 @@ __device__ __forceinline__ void block_scan_chunks(const uint32_t* __restrict__ c
 __device__ __forceinline__ uint32_t query(const uint64_t* __restrict__ bits, const uint32_t* __restrict__ pref,
                                           uint32_t off)
 {
-  uint32_t w = off / 240;
-  uint32_t r = off - w * 240;
-  uint32_t c = w >> 3;
+  const uint32_t w = off / 240;
+  const uint32_t r = off - w * 240;
+  const uint32_t c = w >> 3;
   uint32_t v = pref[c];
   for (uint32_t i = c << 3; i < w; i++) v += __popcll(bits[i]);
   return v + __popcll(bits[w] & mask_le(r));
 }
 
+// Record of one table entry: the offset of the leaf in the segment, bit 30 =
+// negative sign, or REC_NONE when the factor-table filter rejects the entry.
+#define REC_NONE 0xFFFFFFFFu
+template <typename FT>
+__device__ __forceinline__ uint32_t make_record(const SweepArgs& A, const LevelP& P, int64_t e, uint32_t fv,
+                                                const uint16_t* __restrict__ cop, uint64_t low)
+{
+  const uint64_t* xt = A.xp_tab + 3 * (int64_t) P.level;
+  if (!(P.flags & 2)) {
+    if (fv <= P.thr) return REC_NONE;
+    const uint64_t mi = (uint64_t) (P.hi - e);
+    const uint64_t m = 2310 * (mi / 480) + cop[mi % 480];
+    const uint64_t nn = div_xp(xt[0], xt[1], m);
+    return (uint32_t) (nn - low) | ((fv & 1) ? 0u : (1u << 30));
+  }
+  const uint64_t nn = div_xp(xt[0], xt[1], (uint64_t) fv);
+  return (uint32_t) (nn - low);
+}
+
+// exclusive block scan of three int64 values per thread into out[NT + 1] arrays
+template <int NT>
+__device__ __forceinline__ void block_scan3(long long v0, long long v1, long long v2, int64_t* o0, int64_t* o1,
+                                            int64_t* o2, long long (*wt)[3])
+{
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  long long i0 = v0, i1 = v1, i2 = v2;
+  for (int d = 1; d < 32; d <<= 1) {
+    long long t0 = __shfl_up_sync(0xffffffffu, i0, d);
+    long long t1 = __shfl_up_sync(0xffffffffu, i1, d);
+    long long t2 = __shfl_up_sync(0xffffffffu, i2, d);
+    if (lane >= d) { i0 += t0; i1 += t1; i2 += t2; }
+  }
+  if (lane == 31) { wt[warp][0] = i0; wt[warp][1] = i1; wt[warp][2] = i2; }
+  __syncthreads();
+  long long e0 = i0 - v0, e1 = i1 - v1, e2 = i2 - v2;
+  for (int w = 0; w < warp; w++) { e0 += wt[w][0]; e1 += wt[w][1]; e2 += wt[w][2]; }
+  o0[tid] = e0; o1[tid] = e1; o2[tid] = e2;
+  if (tid == NT - 1) { o0[NT] = e0 + v0; o1[NT] = e1 + v1; o2[NT] = e2 + v2; }
+}
+
 template <typename FT, int NT>
-__global__ void __launch_bounds__(NT) k_sweep(const SweepArgs A)
+__global__ void __launch_bounds__(NT, (NT >= 512) ? 2 : ((NT >= 256) ? 3 : 4)) k_sweep(const SweepArgs A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nch = A.words >> 3;
   uint64_t* bits = (uint64_t*) smem_raw;
-  uint32_t* ccount = (uint32_t*) (bits + A.words);
+  uint64_t* pat = bits + A.words;                      // wheel patterns of the primes 7..61
+  int64_t* loff = (int64_t*) (pat + PAT_WORDS);        // record offsets of the batch levels
+  int64_t* hoff = loff + (NT + 1);                     // cross-off co-factor offsets
+  int64_t* rpre = hoff + (NT + 1);                     // prefix of the formula counts
+  uint32_t* ccount = (uint32_t*) (rpre + (NT + 1));
   uint32_t* pref = ccount + nch;
   LevelP* lp = (LevelP*) (pref + nch);
-  uint16_t* cop = (uint16_t*) (lp + NT);
+  uint32_t* rec = (uint32_t*) (lp + NT);
+  uint16_t* runend = (uint16_t*) (rec + A.rec_cap);    // end of the run of leafless levels from i
+  uint16_t* cop = runend + NT;
 
   __shared__ int s_ws;
   __shared__ int s_smu;
@@ -462,14 +517,31 @@ __global__ void __launch_bounds__(NT) k_sweep(const SweepArgs A)
   __shared__ uint32_t s_rem[3];
   __shared__ uint32_t s_total;
   __shared__ uint32_t wtmp[32];
+  __shared__ long long wt3[32][3];
+  __shared__ int s_brk[32];
   __shared__ long long s_red[NT / 32];
   __shared__ unsigned long long s_ctr[4];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const FT* __restrict__ factor = (const FT*) A.factor;
   const u128 x = ((u128) A.x_hi << 64) | A.x_lo;
   const int cols = A.bglob + 1;
+  const int cap = A.rec_cap;
+  const FT* __restrict__ factor = (const FT*) A.factor;
   for (int i = tid; i < 480; i += NT) cop[i] = A.coprime[i];
+  // wheel patterns: word r of prime p keeps the numbers 240 r + {1,7,..,29}
+  // (mod 240 p) that p does not divide
+  for (int i = tid; i < PAT_WORDS; i += NT) {
+    int k = 0, base = 0;
+    while (k < NSMALL - 1 && i >= base + c_small_p[k]) { base += c_small_p[k]; k++; }
+    const uint32_t p = c_small_p[k];
+    const uint32_t r = (uint32_t) (i - base);
+    uint64_t w = ~0ull;
+    for (int j = 0; j < 64; j++) {
+      const uint32_t v = 240 * r + 30 * (j >> 3) + woff(j & 7);
+      if (v % p == 0) w &= ~(1ull << j);
+    }
+    pat[i] = w;
+  }
   if (tid < 4) s_ctr[tid] = 0;
 
   for (;;) {
@@ -479,22 +551,22 @@ __global__ void __launch_bounds__(NT) k_sweep(const SweepArgs A)
     const int ws = s_ws;
     if (ws >= A.wave_len) break;
     const int64_t s = A.wave_first + ws;
-    const int64_t low = s * A.seg;
-    const int64_t high = dmin(low + A.seg, A.L);
+    const int64_t low = A.seglo[s];
+    const int64_t high = A.seglo[s + 1];
     const int64_t low1 = dmax(low, 1);
 
     // level bounds of this segment (chunk bounds of D.cpp:83-94 / S2_hard.cpp:64-71)
     int64_t bmin_leaf, bmax_leaf, bcnt;
     if (A.gourdon) {
-      bmax_leaf = dpi(A.pitab, (uint64_t) dmin(dmin(disqrt(x / (uint64_t) low1), disqrt((u128) high)), A.x_star));
+      bmax_leaf = dpi(A.pitab, (uint64_t) dmin(dmin(disqrt(div128(x, (uint64_t) low1)), disqrt((u128) high)), A.x_star));
       bmin_leaf = dpi(A.pitab, (uint64_t) dmin(A.L / high, A.x_star));
-      bcnt = dpi(A.pitab, (uint64_t) dmin(disqrt(x / (uint64_t) high), A.x_star));
+      bcnt = dpi(A.pitab, (uint64_t) dmin(disqrt(div128(x, (uint64_t) high)), A.x_star));
     } else {
       bmax_leaf = (high <= A.y) ? A.pi_sqrt
-          : dpi(A.pitab, (uint64_t) dmin(dmin(disqrt(x / (uint64_t) low1), disqrt((u128) A.z)), A.y));
+          : dpi(A.pitab, (uint64_t) dmin(dmin(disqrt(div128(x, (uint64_t) low1)), disqrt((u128) A.z)), A.y));
       uint64_t pmax = bmax_leaf > 0 ? A.primes[bmax_leaf] : 0;
       bmin_leaf = dpi(A.pitab, (uint64_t) dmin(A.z / high, (int64_t) pmax));
-      bcnt = dmax(A.pi_sqrt, dpi(A.pitab, (uint64_t) dmin(dmin(disqrt(x / (uint64_t) high), disqrt((u128) A.z)), A.y)));
+      bcnt = dmax(A.pi_sqrt, dpi(A.pitab, (uint64_t) dmin(dmin(disqrt(div128(x, (uint64_t) high)), disqrt((u128) A.z)), A.y)));
     }
     bmin_leaf = dmax(A.k, bmin_leaf) + 1;
     const int Bs = (int) dmin(dmax(bmax_leaf, bcnt), (int64_t) A.bglob);
@@ -517,7 +589,7 @@ __global__ void __launch_bounds__(NT) k_sweep(const SweepArgs A)
         ccount[c] = t;
         part += t;
       }
-      for (int d = 16; d > 0; d >>= 1) part += __shfl_down_sync(0xffffffffu, part, d);
+      part = __reduce_add_sync(0xffffffffu, part);
       if (lane == 0) atomicAdd(&s_total, part);
     }
     __syncthreads();
@@ -528,14 +600,16 @@ __global__ void __launch_bounds__(NT) k_sweep(const SweepArgs A)
 
     for (int b0 = 1; b0 <= Bs; b0 += NT) {
       // ---- per-level parameters of levels b0 .. b0+NT-1, one thread each
+      int64_t E = 0;
+      uint32_t fcnt = 0;
       {
         const int b = b0 + tid;
         LevelP P;
-        P.lo = P.hi = 0; P.jlo = 0; P.jn = 0; P.prime = 0; P.thr = 0; P.flags = 0;
+        P.lo = P.hi = 0; P.jlo = 0; P.jn = 0; P.prime = 0; P.thr = 0; P.flags = 0; P.level = b; P.fcount = 0;
         if (b <= Bs) {
           const uint64_t p = A.primes[b];
           P.prime = (uint32_t) p;
-          if (p >= 7) {
+          if (p >= 64) {
             uint64_t qlo = ((uint64_t) low + p - 1) / p;
             if (qlo < 1) qlo = 1;
             uint64_t qhi = ((uint64_t) high - 1) / p;
@@ -543,6 +617,19 @@ __global__ void __launch_bounds__(NT) k_sweep(const SweepArgs A)
               P.jlo = cnt_le(qlo - 1);
               P.jn = (uint32_t) (cnt_le(qhi) - P.jlo);
             }
+            // p^3 >= high: the numbers of the segment whose least prime factor
+            // is p are p itself and p*q for primes q >= p, so the count of
+            // level b follows from the PiTable
+            if ((u128) p * p * p >= (u128) high && (int64_t) qhi <= A.pi_max) {
+              uint32_t f = ((uint64_t) low <= p && p < (uint64_t) high) ? 1u : 0u;
+              const uint64_t qa = qlo > p ? qlo : p;
+              if (qhi >= qa) f += (uint32_t) (dpi(A.pitab, qhi) - dpi(A.pitab, qa - 1));
+              P.fcount = f;
+              P.flags |= 8;
+            }
+          } else if (p >= 7) {
+            P.jlo = (uint64_t) ((low / 240) % p);   // pattern phase of the first word
+            P.flags |= 4;
           }
           if (b >= bmin_leaf && b <= bmax_leaf) {
             const uint64_t* xt = A.xp_tab + 3 * b;
@@ -568,7 +655,7 @@ __global__ void __launch_bounds__(NT) k_sweep(const SweepArgs A)
               else {
                 P.lo = 480 * (min_m / 2310) + A.cindex[min_m % 2310];
                 P.hi = 480 * (max_m / 2310) + A.cindex[max_m % 2310];
-                if (P.hi > P.lo) P.flags = 1;
+                if (P.hi > P.lo) P.flags |= 1;
               }
             } else {
               int64_t xp_low = divcap(xp, (uint64_t) low1, A.y);
@@ -586,77 +673,203 @@ __global__ void __launch_bounds__(NT) k_sweep(const SweepArgs A)
               else {
                 P.lo = dpi(A.pitab, (uint64_t) dmin(min_hard, A.pi_max));
                 P.hi = l;
-                if (P.hi > P.lo) P.flags = 3;
+                if (P.hi > P.lo) P.flags |= 3;
               }
             }
             if (stop) atomicMin(&s_stop, b);
+            if (P.flags & 1) E = P.hi - P.lo;
           }
         }
+        fcnt = P.fcount;
         lp[tid] = P;
       }
       __syncthreads();
-      const int bend = (int) dmin(b0 + NT - 1, Bs);
-      const int stop_at = s_stop;
-      for (int b = b0; b <= bend; b++) {
-        if (tid == 0) A.cnt[(int64_t) ws * cols + b] = total;
-        const LevelP P = lp[b - b0];
-        if ((P.flags & 1) && b < stop_at) {
-          if (dirty) { block_scan_chunks<NT>(ccount, pref, nch, wtmp); dirty = false; }
-          const uint64_t* xt = A.xp_tab + 3 * b;
-          const uint64_t xlo = xt[0], xhi = xt[1];
-          int smu_t = 0;
-          if (!(P.flags & 2)) {
-            const uint32_t thr = P.thr;
-            for (int64_t mi = P.hi - tid; mi > P.lo; mi -= NT) {
-              const uint32_t f = (uint32_t) factor[mi];
-              if (f > thr) {
-                const uint64_t m = 2310 * (uint64_t) (mi / 480) + cop[mi % 480];
-                const uint64_t n = div_xp(xlo, xhi, m);
-                const uint32_t c = query(bits, pref, (uint32_t) (n - (uint64_t) low));
-                const int sg = (f & 1) ? 1 : -1;
-                lsum += sg * (long long) c;
-                smu_t += sg;
-                nleaves++;
+      const int nb = (int) dmin(NT, (int64_t) (Bs - b0 + 1));
+      {
+        // goto next_segment (D.cpp:131-132): no leaves from s_stop on
+        const bool has_leaves = (b0 + tid < s_stop) && E > 0;
+        if (!has_leaves) E = 0;
+        const uint32_t jn = lp[tid].jn;
+        // flat offsets of records, run cross-off co-factors and formula counts
+        block_scan3<NT>(E, (lp[tid].flags & 8) ? (long long) jn : 0, (long long) fcnt, loff, hoff, rpre, wt3);
+        // runs: levels without leaves whose count follows from the formula
+        const bool breaker = (tid >= nb) || has_leaves || !(lp[tid].flags & 8);
+        const unsigned bal = __ballot_sync(0xffffffffu, breaker);
+        if (lane == 0) s_brk[warp] = bal ? warp * 32 + __ffs((int) bal) - 1 : NT;
+        __syncthreads();
+        const unsigned mine = bal & (0xffffffffu << lane);
+        int re;
+        if (mine) re = warp * 32 + __ffs((int) mine) - 1;
+        else {
+          re = NT;
+          for (int w2 = warp + 1; w2 < NT / 32; w2++)
+            if (s_brk[w2] < NT) { re = s_brk[w2]; break; }
+        }
+        runend[tid] = (uint16_t) dmin(re, nb);
+        __syncthreads();
+      }
+      const int64_t total_e = loff[nb];
+
+      int li = 0;          // next batch level to finish
+      int64_t w0 = 0;      // first flat record of the window
+      while (li < nb) {
+        const int64_t wend = w0 + cap;
+        // ---- phase A: the window's leaf records (flat over levels, 4 loads in flight)
+        const int nrec = (int) dmax(0, dmin(wend, total_e) - w0);
+        if (nrec > 0) {
+          for (int f0 = tid; f0 < nrec; f0 += 4 * NT) {
+            int jl[4];
+            int64_t el[4];
+            uint32_t fv[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+              const int f = f0 + u * NT;
+              jl[u] = -1;
+              if (f < nrec) {
+                const int64_t pos = w0 + f;
+                int lo = li, hi = nb - 1;     // last level with loff <= pos
+                while (lo < hi) {
+                  const int mid = (lo + hi + 1) >> 1;
+                  if (loff[mid] <= pos) lo = mid; else hi = mid - 1;
+                }
+                jl[u] = lo;
+                el[u] = pos - loff[lo];
+                const LevelP& Q = lp[lo];
+                fv[u] = (Q.flags & 2) ? __ldg(&A.primes[Q.hi - el[u]]) : (uint32_t) __ldg(&factor[Q.hi - el[u]]);
               }
             }
-            if (tid == 0) nentries += (unsigned long long) (P.hi - P.lo);
-          } else {
-            for (int64_t l = P.hi - tid; l > P.lo; l -= NT) {
-              const uint64_t q = A.primes[l];
-              const uint64_t n = div_xp(xlo, xhi, q);
-              const uint32_t c = query(bits, pref, (uint32_t) (n - (uint64_t) low));
-              lsum += c;
-              smu_t += 1;
-              nleaves++;
-              ntwo++;
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+              const int f = f0 + u * NT;
+              if (jl[u] >= 0) {
+                const LevelP& Q = lp[jl[u]];
+                const uint32_t r = make_record<FT>(A, Q, el[u], fv[u], cop, (uint64_t) low);
+                rec[f] = r;
+                if (r != REC_NONE) { nleaves++; if (Q.flags & 2) ntwo++; }
+              }
             }
           }
-          for (int d = 16; d > 0; d >>= 1) smu_t += __shfl_down_sync(0xffffffffu, smu_t, d);
-          if (lane == 0 && smu_t) atomicAdd(&s_smu, smu_t);
-          __syncthreads();
-          if (tid == 0) { A.smu[(int64_t) ws * cols + b] = s_smu; s_smu = 0; }
-        }
-        // ---- cross off p_b and its multiples, count the bits removed first
-        if (P.jn) {
-          const uint64_t p = P.prime;
-          uint32_t rem = 0;
-          for (uint32_t j = tid; j < P.jn; j += NT) {
-            const uint64_t jj = P.jlo + j;
-            const uint64_t q = 30 * (jj >> 3) + woff((uint32_t) (jj & 7));
-            const uint32_t off = (uint32_t) (p * q - (uint64_t) low);
-            const uint32_t w = off / 240, r = off - w * 240;
-            const uint64_t m = 1ull << bit_of(r);
-            const uint64_t old = atomicAnd((unsigned long long*) &bits[w], ~m);
-            if (old & m) { rem++; atomicSub(&ccount[w >> 3], 1u); }
+          if (tid == 0) {
+            for (int j = li; j < nb; j++) {
+              const int64_t a = dmax(loff[j], w0), e2 = dmin(loff[j + 1], wend);
+              if (a >= wend) break;
+              if (e2 > a && !(lp[j].flags & 2)) nentries += (unsigned long long) (e2 - a);
+            }
           }
-          for (int d = 16; d > 0; d >>= 1) rem += __shfl_down_sync(0xffffffffu, rem, d);
-          if (lane == 0 && rem) atomicAdd(&s_rem[b % 3], rem);
+          __syncthreads();
         }
-        __syncthreads();
-        const uint32_t r = s_rem[b % 3];
-        total -= r;
-        if (r) dirty = true;
-        if (tid == 0) s_rem[(b + 2) % 3] = 0;
+        // ---- phase B: levels in order
+        while (li < nb) {
+          const int re = runend[li];
+          if (re > li) {
+            // a run of leafless levels li .. re-1 with formula counts: their
+            // counts from the prefix, all their multiples crossed off at once
+            const int64_t r0 = rpre[li];
+            for (int t = tid; t < re - li; t += NT)
+              A.cnt[(int64_t) ws * cols + b0 + li + t] = total - (uint32_t) (rpre[li + t] - r0);
+            const int64_t h0 = hoff[li], h1 = hoff[re];
+            for (int64_t h = h0 + tid; h < h1; h += NT) {
+              int lo = li, hi = re - 1;       // last level with hoff <= h
+              while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (hoff[mid] <= h) lo = mid; else hi = mid - 1;
+              }
+              const LevelP& Q = lp[lo];
+              const uint64_t jj = Q.jlo + (uint64_t) (h - hoff[lo]);
+              const uint64_t q = 30 * (jj >> 3) + woff((uint32_t) (jj & 7));
+              const uint32_t off = (uint32_t) ((uint64_t) Q.prime * q - (uint64_t) low);
+              const uint32_t w = off / 240, rr = off - w * 240;
+              const uint64_t m = 1ull << bit_of(rr);
+              const uint64_t old = atomicAnd((unsigned long long*) &bits[w], ~m);
+              if (old & m) atomicSub(&ccount[w >> 3], 1u);
+            }
+            const uint32_t removed = (uint32_t) (rpre[re] - r0);
+            total -= removed;
+            if (h1 > h0) dirty = true;
+            li = re;
+            __syncthreads();
+            continue;
+          }
+          const int64_t la = loff[li], lz = loff[li + 1];
+          if (lz > la && la >= wend) break;               // records start in a later window
+          const int l = b0 + li;
+          if (la >= w0 && tid == 0) A.cnt[(int64_t) ws * cols + l] = total;
+          const int ra = (int) (dmax(la, w0) - w0), rb = (int) (dmin(lz, wend) - w0);
+          if (rb > ra) {
+            if (dirty) { block_scan_chunks<NT>(ccount, pref, nch, wtmp); dirty = false; }
+            if (ra + 32 * warp < rb) {
+              int smu_t = 0;
+              for (int k2 = ra + tid; k2 < rb; k2 += NT) {
+                const uint32_t r = rec[k2];
+                if (r != REC_NONE) {
+                  const uint32_t c = query(bits, pref, r & 0x3FFFFFFFu);
+                  if (r & (1u << 30)) { lsum -= c; smu_t--; }
+                  else { lsum += c; smu_t++; }
+                }
+              }
+              smu_t = __reduce_add_sync(0xffffffffu, smu_t);
+              if (lane == 0 && smu_t) atomicAdd(&s_smu, smu_t);
+            }
+            __syncthreads();
+            if (lz <= wend && tid == 0) { A.smu[(int64_t) ws * cols + l] = s_smu; s_smu = 0; }
+          }
+          if (lz > wend) break;                            // the level continues in the next window
+          // ---- cross off p_l and its multiples, count the numbers removed first
+          const LevelP& P = lp[li];
+          uint32_t rem = 0;
+          if (P.flags & 4) {
+            // small prime: AND with its wheel pattern, one owner thread per word
+            const uint32_t p = P.prime;
+            int po = 0;
+            for (int k = 0; c_small_p[k] != p; k++) po += c_small_p[k];
+            uint32_t r = (uint32_t) ((P.jlo + tid) % p);
+            const uint32_t step = NT % p;
+            for (int w = tid; w < A.words; w += NT) {
+              uint32_t d = 0;
+              if (w < wused) {
+                const uint64_t old = bits[w];
+                const uint64_t nw = old & pat[po + r];
+                if (nw != old) { bits[w] = nw; d = __popcll(old ^ nw); }
+              }
+              rem += d;
+              // 8 consecutive lanes own the 8 words of one chunk
+              d += __shfl_down_sync(0xffffffffu, d, 4, 8);
+              d += __shfl_down_sync(0xffffffffu, d, 2, 8);
+              d += __shfl_down_sync(0xffffffffu, d, 1, 8);
+              if ((lane & 7) == 0 && d) ccount[w >> 3] -= d;
+              r += step;
+              if (r >= p) r -= p;
+            }
+          } else if (P.jn) {
+            if (32 * warp < (int) P.jn) {
+              const uint64_t p = P.prime;
+              for (uint32_t j = tid; j < P.jn; j += NT) {
+                const uint64_t jj = P.jlo + j;
+                const uint64_t q = 30 * (jj >> 3) + woff((uint32_t) (jj & 7));
+                const uint32_t off = (uint32_t) (p * q - (uint64_t) low);
+                const uint32_t w = off / 240, rr = off - w * 240;
+                const uint64_t m = 1ull << bit_of(rr);
+                const uint64_t old = atomicAnd((unsigned long long*) &bits[w], ~m);
+                if (old & m) { rem++; atomicSub(&ccount[w >> 3], 1u); }
+              }
+            }
+          }
+          if (P.flags & 8) {
+            __syncthreads();
+            total -= P.fcount;
+            if (P.jn) dirty = true;
+          } else {
+            rem = __reduce_add_sync(0xffffffffu, rem);
+            if (lane == 0 && rem) atomicAdd(&s_rem[l % 3], rem);
+            __syncthreads();
+            const uint32_t rr = s_rem[l % 3];
+            total -= rr;
+            if (rr) dirty = true;
+            if (tid == 0) s_rem[(l + 2) % 3] = 0;
+          }
+          li++;
+        }
+        w0 = wend;
       }
     }
     // segment result
@@ -908,14 +1121,114 @@ void ensure_factor_dr(Ctx& c, int64_t y, cudaStream_t s)
 }
 
 template <typename FT, int NT>
+static void set_sweep_attr(size_t smem)
+{
+  static size_t set = 0;
+  if (set < smem) {
+    PCG_CUDA(cudaFuncSetAttribute(k_sweep<FT, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+    set = smem;
+  }
+}
+
+template <typename FT, int NT>
+static void occupancy_sweep(int* occ, size_t smem)
+{
+  set_sweep_attr<FT, NT>(smem);
+  PCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, k_sweep<FT, NT>, NT, smem));
+}
+
+template <typename FT, int NT>
 static void launch_sweep(const SweepArgs& a, int grid, size_t smem, cudaStream_t s)
 {
-  static bool attr_set = false;
-  if (!attr_set) {
-    PCG_CUDA(cudaFuncSetAttribute(k_sweep<FT, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr_set = true;
-  }
+  set_sweep_attr<FT, NT>(smem);
   k_sweep<FT, NT><<<grid, NT, smem, s>>>(a);
+}
+
+// Segment planner (the role of LoadBalancerS2's growing segment sizes,
+// src/LoadBalancerS2.cpp:195-264, decided up front): an analytic estimate of
+// the leaves of every family per interval (m-range length times the density
+// of square-free numbers without prime factors <= p_b, or the prime density
+// for the p_b * p_l leaves) plus a per-level cost, integrated on a geometric
+// grid; segments are cut at equal estimated cost, never longer than smax.
+static std::vector<int64_t> plan_segments(const SweepProblem& pb, const Tables& t, int64_t L, int64_t x_star,
+                                          int64_t pi_sqrt, int64_t bglob, int64_t smax, int grid)
+{
+  const double x = (double) pb.x;
+  const double y = (double) pb.y, z = (double) pb.z;
+  const int G = 1200;
+  std::vector<double> g;
+  g.push_back(0);
+  double a0 = 240;
+  double ratio = std::pow((double) L / a0, 1.0 / (G - 1));
+  for (int i = 0; i < G; i++) g.push_back(std::min((double) L, a0 * std::pow(ratio, i)));
+  g.back() = (double) L;
+  std::vector<double> pr((size_t) bglob + 1), dens((size_t) bglob + 1);
+  for (int64_t b = 1; b <= bglob; b++) {
+    pr[b] = (double) t.h_primes[(size_t) b];
+    dens[b] = 0.56 / std::log(std::max(pr[b], 3.0));
+  }
+  auto leaves = [&](double lo, double hi) {
+    double sum = 0;
+    double l1 = std::max(lo, 1.0);
+    for (int64_t b = pb.k + 1; b <= bglob; b++) {
+      const double p = pr[b], xp = x / p;
+      double mlo, mhi;
+      if (pb.gourdon) {
+        if (b <= pi_sqrt) { mlo = std::max(z / p, xp / hi); mhi = std::min({xp / (p * p), z, xp / l1}); }
+        else { mlo = std::max(p, xp / hi); mhi = std::min({xp / (p * p), y, xp / l1}); }
+      } else {
+        if (b <= pi_sqrt) { mlo = std::max(y / p, xp / hi); mhi = std::min(xp / l1, y); }
+        else { mlo = std::max(p, xp / hi); mhi = std::min({xp / l1, y, z / p}); }
+      }
+      if (mhi <= mlo) continue;
+      sum += (b <= pi_sqrt) ? (mhi - mlo) * dens[b] : (mhi - mlo) / std::log(std::max(mhi, 3.0));
+    }
+    return sum;
+  };
+  auto levels = [&](double a) {
+    double lim = pb.gourdon ? std::min((double) x_star, std::sqrt(x / std::max(a, 1.0)))
+                            : std::min(std::sqrt(z), std::sqrt(x / std::max(a, 1.0)));
+    return (double) host_pi(t, (uint64_t) std::min(lim, (double) t.prime_limit));
+  };
+  const double c_level = 30.0;
+  std::vector<double> cum(g.size(), 0.0);
+  for (size_t i = 0; i + 1 < g.size(); i++) {
+    double len = g[i + 1] - g[i];
+    double c = len > 0 ? leaves(g[i], g[i + 1]) + c_level * levels(g[i]) * len / (double) smax : 0;
+    cum[i + 1] = cum[i] + c;
+  }
+  const double total = cum.back();
+  const double target = std::max(total / (grid * 6.0), 1.0);
+  // cumulative cost at n (linear inside a grid cell)
+  auto C = [&](double n) {
+    size_t i = std::upper_bound(g.begin(), g.end(), n) - g.begin();
+    if (i == 0) return 0.0;
+    if (i >= g.size()) return total;
+    double f = (g[i] > g[i - 1]) ? (n - g[i - 1]) / (g[i] - g[i - 1]) : 0;
+    return cum[i - 1] + f * (cum[i] - cum[i - 1]);
+  };
+  std::vector<int64_t> seg;
+  int64_t a = 0;
+  seg.push_back(0);
+  while (a < L) {
+    double ca = C((double) a);
+    int64_t lo = a + 240, hi = std::min(a + smax, L);
+    if (hi <= lo) { a = std::min(a + smax, L); seg.push_back(a); continue; }
+    // largest end with cost <= target (binary search on multiples of 240)
+    int64_t best = lo;
+    if (C((double) hi) - ca <= target) best = hi;
+    else {
+      int64_t l = lo / 240, h = hi / 240;
+      while (l < h) {
+        int64_t m = (l + h + 1) / 2;
+        if (C((double) (m * 240)) - ca <= target) l = m; else h = m - 1;
+      }
+      best = std::max(lo, l * 240);
+    }
+    a = std::min(best, L);
+    seg.push_back(a);
+  }
+  return seg;
 }
 
 SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaStream_t s)
@@ -963,17 +1276,34 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
     xp[3 * b + 2] = q3 > (u128) INT64_MAX ? (uint64_t) INT64_MAX : (uint64_t) q3;
   }
 
-  // tuning
+  // tuning: threads per CTA, bitmap words per CTA, leaf-record capacity,
+  // resident CTAs per SM
+  const int NT = (tune.cta_threads == 512 || tune.cta_threads == 128) ? tune.cta_threads : 256;
   int words = tune.segment_words > 0 ? tune.segment_words : 8192;
-  const int NT = 512;
   words = std::max(words, 8 * NT);
   words = (words + 8 * NT - 1) / (8 * NT) * (8 * NT);
-  int ctas = tune.ctas_per_sm > 0 ? tune.ctas_per_sm : 2;
-  int64_t seg = (int64_t) words * 240;
-  int64_t nseg = (L + seg - 1) / seg;
+  const int cap = 4096;
+  size_t smem = (size_t) words * 8 + PAT_WORDS * 8 + (size_t) (NT + 1) * 8 * 3 + (size_t) (words / 8) * 8 +
+                sizeof(LevelP) * NT + (size_t) cap * 4 + (size_t) NT * 2 + 480 * 2 + 16;
+  if (smem > c.smem_optin) fail(PCG_EINVAL, "segment too large for shared memory");
+  int fbytes = pb.gourdon ? c.tab.fd_bytes : c.tab.fr_bytes;
+  auto occupancy = [&](int* occ) {
+    if (NT == 512) { if (fbytes == 2) occupancy_sweep<uint16_t, 512>(occ, smem); else occupancy_sweep<uint32_t, 512>(occ, smem); }
+    else if (NT == 256) { if (fbytes == 2) occupancy_sweep<uint16_t, 256>(occ, smem); else occupancy_sweep<uint32_t, 256>(occ, smem); }
+    else { if (fbytes == 2) occupancy_sweep<uint16_t, 128>(occ, smem); else occupancy_sweep<uint32_t, 128>(occ, smem); }
+  };
+  int occ = 0;
+  occupancy(&occ);
+  int ctas = tune.ctas_per_sm > 0 ? std::min(tune.ctas_per_sm, std::max(occ, 1)) : std::max(occ, 1);
   int grid = c.num_sms * ctas;
-  size_t smem = (size_t) words * 8 + (size_t) (words / 8) * 8 + sizeof(LevelP) * NT + 480 * 2 + 16;
-  if (smem > 200 * 1024) fail(PCG_EINVAL, "segment too large for shared memory");
+
+  // segment table: small segments where leaves are dense, full ones elsewhere
+  std::vector<int64_t> seglo = plan_segments(pb, c.tab, L, x_star, pi_sqrt, bglob, (int64_t) words * 240, grid);
+  int64_t nseg = (int64_t) seglo.size() - 1;
+  DevBuf segbuf;
+  segbuf.alloc(seglo.size() * 8);
+  PCG_CUDA(cudaMemcpyAsync(segbuf.p, seglo.data(), seglo.size() * 8, cudaMemcpyHostToDevice, s));
+
   int64_t wave_cap = (int64_t) grid * 8;
   // budget of the C/M matrices: 1 GiB
   int64_t max_rows = std::max<int64_t>(1, (int64_t) (1ull << 30) / ((int64_t) cols * 8));
@@ -994,7 +1324,7 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   PCG_CUDA(cudaMemsetAsync(c.acc.p, 0, (size_t) cols * 16, s));
   PCG_CUDA(cudaMemsetAsync(c.misc.p, 0, 4096, s));
   unsigned long long* d_counters = (unsigned long long*) c.misc.p;
-  int* d_queue = (int*) ((char*) c.misc.p + 64);
+  int* d_queue = (int*) ((char*) c.misc.p + 256);   // after the 32 counters
 
   SweepArgs a;
   memset(&a, 0, sizeof(a));
@@ -1005,8 +1335,9 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   a.k = pb.k;
   a.L = L;
   a.x_star = x_star;
-  a.seg = seg;
+  a.seglo = segbuf.as<int64_t>();
   a.words = words;
+  a.rec_cap = cap;
   a.gourdon = pb.gourdon;
   a.pi_sqrt = (int) pi_sqrt;
   a.bglob = (int) bglob;
@@ -1015,7 +1346,6 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   a.pitab = c.tab.pitab.as<uint64_t>();
   a.pi_max = c.tab.prime_limit;
   a.factor = pb.gourdon ? c.tab.factor_d.p : c.tab.factor_dr.p;
-  int fbytes = pb.gourdon ? c.tab.fd_bytes : c.tab.fr_bytes;
   a.xp_tab = d_xp;
   a.coprime = c.tab.coprime.as<uint16_t>();
   a.cindex = c.tab.cindex.as<int16_t>();
@@ -1026,7 +1356,7 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
 
   PCG_CUDA(cudaEventRecord(c.ev[0], s));
   uint64_t launches = 0;
-  float ms_sweep = 0, ms_comb = 0;
+  float ms_sweep = 0;
   int waves = 0;
   for (int64_t first = 0; first < nseg; first += wave_len) {
     int wl = (int) std::min<int64_t>(wave_len, nseg - first);
@@ -1037,9 +1367,17 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
     PCG_CUDA(cudaMemsetAsync(c.smu.p, 0, (size_t) wl * cols * 4, s));
     if (waves % 16 == 0 && waves > 0) PCG_CUDA(cudaMemsetAsync(d_queue, 0, 64, s));
     int g = (int) std::min<int64_t>(grid, wl);
-    if (fbytes == 2) launch_sweep<uint16_t, 512>(a, g, smem, s);
-    else launch_sweep<uint32_t, 512>(a, g, smem, s);
+    if ((size_t) (2 * waves + 2) > c.kev.size()) {
+      size_t n0 = c.kev.size();
+      c.kev.resize((size_t) (2 * waves + 2) * 2);
+      for (size_t i = n0; i < c.kev.size(); i++) PCG_CUDA(cudaEventCreate(&c.kev[i]));
+    }
+    PCG_CUDA(cudaEventRecord(c.kev[2 * waves], s));
+    if (NT == 512) { if (fbytes == 2) launch_sweep<uint16_t, 512>(a, g, smem, s); else launch_sweep<uint32_t, 512>(a, g, smem, s); }
+    else if (NT == 256) { if (fbytes == 2) launch_sweep<uint16_t, 256>(a, g, smem, s); else launch_sweep<uint32_t, 256>(a, g, smem, s); }
+    else { if (fbytes == 2) launch_sweep<uint16_t, 128>(a, g, smem, s); else launch_sweep<uint32_t, 128>(a, g, smem, s); }
     PCG_CUDA(cudaGetLastError());
+    PCG_CUDA(cudaEventRecord(c.kev[2 * waves + 1], s));
     k_combine<<<(cols + 255) / 256, 256, 0, s>>>(a.cnt, a.smu, wl, cols, c.run.as<int64_t>(), c.acc.as<i128>());
     k_segsum<<<1, 1024, 0, s>>>(a.segsum, wl, c.acc.as<i128>());
     PCG_CUDA(cudaGetLastError());
@@ -1053,6 +1391,16 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   PCG_CUDA(cudaMemcpyAsync(ctr, d_counters, sizeof(ctr), cudaMemcpyDeviceToHost, s));
   PCG_CUDA(cudaStreamSynchronize(s));
   PCG_CUDA(cudaEventElapsedTime(&ms_sweep, c.ev[0], c.ev[1]));
+  double kms = 0;
+  for (int w = 0; w < waves; w++) {
+    float m = 0;
+    PCG_CUDA(cudaEventElapsedTime(&m, c.kev[2 * w], c.kev[2 * w + 1]));
+    kms += m;
+  }
+  st.sweep_kernel_ms = kms;
+  st.sweep_launches = (uint64_t) waves;
+  st.h2d_bytes = xp.size() * 8 + seglo.size() * 8;
+  st.d2h_bytes = (uint64_t) cols * 16 + sizeof(ctr);
   i128 sum = 0;
   for (int b = 0; b < cols; b++) sum += acc[(size_t) b];
   res.sum = sum;
@@ -1063,7 +1411,7 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   st.segments = (uint64_t) nseg;
   st.kernel_launches = launches;
   st.sweep_ms = ms_sweep;
-  st.combine_ms = ms_comb;
+  st.combine_ms = ms_sweep - kms;
   st.segment_words = words;
   st.ctas_per_sm = ctas;
   st.threads_per_cta = NT;

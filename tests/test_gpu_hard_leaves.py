@@ -62,13 +62,17 @@ def test_leaf_count_matches_oracle(pcg, ora):
         assert st["factor_entries"] == st_ref["indices_scanned"], x
 
 
-@pytest.mark.parametrize("words,ctas", [(4096, 1), (4096, 4), (8192, 2), (16384, 1)])
-def test_result_independent_of_tuning(pcg, words, ctas):
+@pytest.mark.parametrize("words,ctas,nt", [(4096, 0, 128), (8192, 0, 256), (4096, 0, 512), (16384, 1, 256),
+                                           (8192, 1, 128)])
+def test_result_independent_of_tuning(pcg, words, ctas, nt):
+    # segment size, CTA width and residency change the segmentation and the
+    # work split; the sums are segmentation independent
     x = 10 ** 15
     p = pcg.gourdon_params(x)
-    assert pcg.D(x, p["y"], p["z"], p["k"], segment_words=words, ctas_per_sm=ctas) == 27248002319287
+    assert pcg.D(x, p["y"], p["z"], p["k"], segment_words=words, ctas_per_sm=ctas, cta_threads=nt) == 27248002319287
     d = pcg.dr_params(x)
-    assert pcg.S2_hard(x, d["y"], d["z"], d["c"], segment_words=words, ctas_per_sm=ctas) == 32272468597257
+    assert pcg.S2_hard(x, d["y"], d["z"], d["c"], segment_words=words, ctas_per_sm=ctas,
+                       cta_threads=nt) == 32272468597257
 
 
 def test_oracle_random_small(pcg, ora):
