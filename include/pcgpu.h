@@ -115,6 +115,24 @@ pcg_status pcg_D(pcg_i128 x, int64_t y, int64_t z, int64_t k,
 pcg_status pcg_S2_hard(pcg_i128 x, int64_t y, int64_t z, int64_t c,
                        const pcg_opts* opts, pcg_i128* out);
 
+/* D(x, y, z, k) without allocating device memory.  No counterpart in the
+ * reference.  For callers that cannot call cudaMalloc when they need the
+ * result: code running while a stream is being captured into a CUDA graph,
+ * request paths of a serving loop that must not touch the allocator, or
+ * processes whose device memory belongs to another framework's pool.  The
+ * tables are inputs: ctx must have been created (pcg_ctx_create, which does
+ * allocate, at set-up time) with a max_x whose tables cover y and z, else
+ * PCG_ERANGE.  All working memory comes from one 64 MiB static device array
+ * that every GPU loading the library holds until exit; a call needing more
+ * (or more than 32768 levels) is rejected with PCG_ERANGE.  The first call on
+ * a device looks up the array's device address, so make it before any stream
+ * capture.  Calls share the array and it keeps the last call's contents
+ * (what must start at zero is cleared on the stream); calls overlapping on
+ * the GPU race, so run them on one stream or one after another.  stream may
+ * be NULL (the context's stream); the result is written to *out on return. */
+pcg_status pcg_D_noalloc(pcg_ctx* ctx, pcg_i128 x, int64_t y, int64_t z, int64_t k,
+                         void* stream, pcg_i128* out);
+
 /* D(x) / S2_hard(x) with the reference's default parameters
  * (the --D / --S2-hard command-line options, src/app/main.cpp:205-246,
  * 435-461).  y, z, k (c) are written when the pointers are non-NULL. */

@@ -386,6 +386,35 @@ pcg_status pcg_S2_hard(pcg_i128 x, int64_t y, int64_t z, int64_t c, const pcg_op
   return hard_leaves(false, x, y, z, c, opts, out);
 }
 
+// Allocation-free D for callers that cannot allocate device memory at call
+// time (see include/pcgpu.h): tables from the context, working memory from
+// the library's static device scratch.
+pcg_status pcg_D_noalloc(pcg_ctx* ctx, pcg_i128 xi, int64_t y, int64_t z, int64_t k, void* stream, pcg_i128* out)
+{
+  if (!out) return PCG_EINVAL;
+  return guard(ctx, [&] {
+    if (!ctx) fail(PCG_EINVAL, "pcg_D_noalloc needs a context created with pcg_ctx_create");
+    Ctx& c = *ctx;
+    c.last_error.clear();
+    if (xi.hi < 0) fail(PCG_EINVAL, "x must be >= 0");
+    u128 x = make_u128(xi);
+    i128 result = 0;
+    if (x >= 1) {
+      check_hard_args(x, y, z, k, true);
+      SweepProblem p;
+      p.gourdon = 1;
+      p.x = x;
+      p.y = y;
+      p.z = z;
+      p.k = k;
+      SweepResult r = run_sweep_noalloc(c, p, stream ? (cudaStream_t) stream : c.stream);
+      result = r.sum;
+      c.last = r.stats;
+    }
+    *out = to_pcg(result);
+  });
+}
+
 pcg_status pcg_D_default(pcg_i128 xi, const pcg_opts* opts, pcg_i128* out, int64_t* y, int64_t* z, int64_t* k)
 {
   int64_t yy = 1, zz = 1, kk = 0, xs = 0;

@@ -119,6 +119,8 @@ struct SweepResult {
 };
 
 SweepResult run_sweep(Ctx& c, const SweepProblem& p, const Tuning& t, cudaStream_t s);
+// D with working memory from a static device array; tables must be resident
+SweepResult run_sweep_noalloc(Ctx& c, const SweepProblem& p, cudaStream_t s);
 
 // ---------------------------------------------------------------- context
 struct Ctx {

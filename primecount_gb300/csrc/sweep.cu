@@ -31,6 +31,8 @@
 #include <cstring>
 #include <chrono>
 #include <algorithm>
+#include <mutex>
+#include <string>
 
 #include "pcg_internal.hpp"
 
@@ -1412,6 +1414,287 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   st.kernel_launches = launches;
   st.sweep_ms = ms_sweep;
   st.combine_ms = ms_sweep - kms;
+  st.segment_words = words;
+  st.ctas_per_sm = ctas;
+  st.threads_per_cta = NT;
+  st.total_ms = now_ms() - t_start;
+  return res;
+}
+
+
+// ================================================================ allocation-free D
+// Some callers cannot allocate device memory at the time they need D(x):
+// code that runs while a CUDA stream is being captured, serving loops that
+// must not touch the allocator on the request path, or hosts whose device
+// memory is owned by another framework's pool.  pcg_D_noalloc serves them:
+// it reads the tables a context built earlier (at set-up, when allocating was
+// allowed) and takes all of its working memory -- the per-(segment, level)
+// count and sign matrices, the segment and x/p tables, the counters and the
+// work queue -- from the file-scope array below.  Every GPU that loads this
+// library holds the array until the process exits.  All calls share it and
+// it keeps the previous call's contents, so everything that must start at
+// zero is cleared on the stream at the start of a call, and two calls whose
+// work overlaps on the GPU (different streams, or different host threads)
+// race on it; calls are serialised on the host by a mutex, but the caller
+// must not overlap them on the device.
+#define PCG_NOALLOC_SCRATCH_BYTES (64ull << 20)
+#define PCG_NOALLOC_MAX_COLS 32768
+#define PCG_NOALLOC_MAX_SEGS (1 << 20)
+static __device__ __align__(256) unsigned char g_noalloc_scratch[PCG_NOALLOC_SCRATCH_BYTES];
+
+// Device address of the scratch array for the current device.  Host code
+// only holds a host-side stand-in for the symbol, so the address comes from
+// cudaGetSymbolAddress, once per device with that device current; the first
+// call on a device does this set-up, so it should come before any stream
+// capture.
+static unsigned char* noalloc_scratch()
+{
+  static std::mutex mu;
+  static unsigned char* addr[64] = {nullptr};
+  int dev = 0;
+  PCG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) fail(PCG_EINVAL, "device index out of range");
+  std::lock_guard<std::mutex> g(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      fail(PCG_ECUDA, std::string("cudaGetSymbolAddress of the no-alloc scratch failed: ") + cudaGetErrorString(e));
+    }
+    addr[dev] = (unsigned char*) p;
+  }
+  return addr[dev];
+}
+
+// The segment planner of run_sweep with fixed-size arrays: same grid, same
+// cost model, segments written to out[0 .. return value].
+static int64_t plan_segments_fixed(const SweepProblem& pb, const Tables& t, int64_t L, int64_t x_star,
+                                   int64_t pi_sqrt, int64_t bglob, int64_t smax, int grid, int64_t* out,
+                                   int64_t max_out)
+{
+  const double x = (double) pb.x;
+  const double y = (double) pb.y, z = (double) pb.z;
+  const int G = 1200;
+  double g[G + 1], cum[G + 1];
+  g[0] = 0;
+  const double a0 = 240;
+  const double ratio = std::pow((double) L / a0, 1.0 / (G - 1));
+  for (int i = 0; i < G; i++) g[i + 1] = std::min((double) L, a0 * std::pow(ratio, i));
+  g[G] = (double) L;
+  auto dens = [&](int64_t b) { return 0.56 / std::log(std::max((double) t.h_primes[(size_t) b], 3.0)); };
+  auto leaves = [&](double lo, double hi) {
+    double sum = 0;
+    double l1 = std::max(lo, 1.0);
+    for (int64_t b = pb.k + 1; b <= bglob; b++) {
+      const double p = (double) t.h_primes[(size_t) b], xp = x / p;
+      double mlo, mhi;
+      if (b <= pi_sqrt) { mlo = std::max(z / p, xp / hi); mhi = std::min({xp / (p * p), z, xp / l1}); }
+      else { mlo = std::max(p, xp / hi); mhi = std::min({xp / (p * p), y, xp / l1}); }
+      if (mhi <= mlo) continue;
+      sum += (b <= pi_sqrt) ? (mhi - mlo) * dens(b) : (mhi - mlo) / std::log(std::max(mhi, 3.0));
+    }
+    return sum;
+  };
+  auto levels = [&](double a) {
+    double lim = std::min((double) x_star, std::sqrt(x / std::max(a, 1.0)));
+    return (double) host_pi(t, (uint64_t) std::min(lim, (double) t.prime_limit));
+  };
+  const double c_level = 30.0;
+  cum[0] = 0;
+  for (int i = 0; i < G; i++) {
+    double len = g[i + 1] - g[i];
+    double c = len > 0 ? leaves(g[i], g[i + 1]) + c_level * levels(g[i]) * len / (double) smax : 0;
+    cum[i + 1] = cum[i] + c;
+  }
+  const double total = cum[G];
+  const double target = std::max(total / (grid * 6.0), 1.0);
+  auto C = [&](double n) {
+    int i = (int) (std::upper_bound(g, g + G + 1, n) - g);
+    if (i == 0) return 0.0;
+    if (i > G) return total;
+    double f = (g[i] > g[i - 1]) ? (n - g[i - 1]) / (g[i] - g[i - 1]) : 0;
+    return cum[i - 1] + f * (cum[i] - cum[i - 1]);
+  };
+  int64_t n = 0;
+  int64_t a = 0;
+  out[n++] = 0;
+  while (a < L) {
+    if (n >= max_out) return -1;
+    double ca = C((double) a);
+    int64_t lo = a + 240, hi = std::min(a + smax, L);
+    if (hi <= lo) { a = std::min(a + smax, L); out[n++] = a; continue; }
+    int64_t best = lo;
+    if (C((double) hi) - ca <= target) best = hi;
+    else {
+      int64_t l = lo / 240, h = hi / 240;
+      while (l < h) {
+        int64_t m = (l + h + 1) / 2;
+        if (C((double) (m * 240)) - ca <= target) l = m; else h = m - 1;
+      }
+      best = std::max(lo, l * 240);
+    }
+    a = std::min(best, L);
+    out[n++] = a;
+  }
+  return n - 1;
+}
+
+SweepResult run_sweep_noalloc(Ctx& c, const SweepProblem& pb, cudaStream_t s)
+{
+  static std::mutex call_mu;
+  static uint64_t h_xp[3 * PCG_NOALLOC_MAX_COLS];
+  static int64_t h_seg[PCG_NOALLOC_MAX_SEGS + 1];
+  static i128 h_acc[PCG_NOALLOC_MAX_COLS];
+  std::lock_guard<std::mutex> guard(call_mu);
+  SweepResult res;
+  pcg_stats& st = res.stats;
+  double t_start = now_ms();
+  unsigned char* scratch = noalloc_scratch();
+  const u128 x = pb.x;
+  const Tables& T = c.tab;
+  // the tables are inputs: they must already be resident (no building here)
+  if (!pb.gourdon) fail(PCG_EINVAL, "pcg_D_noalloc computes D only");
+  if (T.prime_limit < pb.y || !(T.fd_z >= pb.z && (T.fd_y == pb.y || (pb.y >= pb.z && T.fd_y >= pb.z))))
+    fail(PCG_ERANGE, "pcg_D_noalloc: the context's resident tables do not cover y = " + std::to_string(pb.y) +
+                         ", z = " + std::to_string(pb.z) + " (create the context with a larger max_x)");
+  const int64_t L = (int64_t) (x / (u128) pb.z);
+  const int64_t x_star = x_star_gourdon(x, pb.y);
+  const int64_t pi_sqrt = host_pi(T, (uint64_t) isqrt((u128) pb.z));
+  const int64_t bglob = host_pi(T, (uint64_t) x_star);
+  if (L <= 0 || bglob < 1) {
+    st.total_ms = now_ms() - t_start;
+    return res;
+  }
+  const int cols = (int) bglob + 1;
+  if (cols > PCG_NOALLOC_MAX_COLS)
+    fail(PCG_ERANGE, "pcg_D_noalloc: " + std::to_string(cols) + " levels exceed the maximum of " +
+                         std::to_string(PCG_NOALLOC_MAX_COLS));
+  for (int64_t b = 1; b <= bglob; b++) {
+    u128 p = T.h_primes[(size_t) b];
+    u128 q = x / p;
+    u128 q3 = q / (p * p);
+    h_xp[3 * b] = (uint64_t) q;
+    h_xp[3 * b + 1] = (uint64_t) (q >> 64);
+    h_xp[3 * b + 2] = q3 > (u128) INT64_MAX ? (uint64_t) INT64_MAX : (uint64_t) q3;
+  }
+  h_xp[0] = h_xp[1] = h_xp[2] = 0;
+
+  const int NT = 256;
+  const int words = 8192;
+  const int cap = 4096;
+  size_t smem = (size_t) words * 8 + PAT_WORDS * 8 + (size_t) (NT + 1) * 8 * 3 + (size_t) (words / 8) * 8 +
+                sizeof(LevelP) * NT + (size_t) cap * 4 + (size_t) NT * 2 + 480 * 2 + 16;
+  const int fbytes = T.fd_bytes;
+  int occ = 0;
+  if (fbytes == 2) occupancy_sweep<uint16_t, 256>(&occ, smem);
+  else occupancy_sweep<uint32_t, 256>(&occ, smem);
+  const int ctas = std::max(occ, 1);
+  const int grid = c.num_sms * ctas;
+  const int64_t nseg = plan_segments_fixed(pb, T, L, x_star, pi_sqrt, bglob, (int64_t) words * 240, grid, h_seg,
+                                           PCG_NOALLOC_MAX_SEGS);
+  if (nseg < 0) fail(PCG_ERANGE, "pcg_D_noalloc: too many segments for the fixed segment table");
+
+  // carve the scratch: counters and queue, x/p table, segment table, run,
+  // acc, segsum, then the count and sign matrices with as many rows as fit
+  auto align = [](size_t v) { return (v + 255) & ~(size_t) 255; };
+  size_t off = 0;
+  unsigned long long* d_counters = (unsigned long long*) (scratch + off);
+  int* d_queue = (int*) (scratch + off + 256);
+  off = align(off + 4096);
+  uint64_t* d_xp = (uint64_t*) (scratch + off);
+  off = align(off + (size_t) cols * 24);
+  int64_t* d_seg = (int64_t*) (scratch + off);
+  off = align(off + (size_t) (nseg + 1) * 8);
+  int64_t* d_run = (int64_t*) (scratch + off);
+  off = align(off + (size_t) cols * 8);
+  i128* d_acc = (i128*) (scratch + off);
+  off = align(off + (size_t) cols * 16);
+  const size_t fixed = off;
+  const size_t per_row = (size_t) cols * 8 + 8 + 512;
+  if (fixed + per_row > PCG_NOALLOC_SCRATCH_BYTES)
+    fail(PCG_ERANGE, "pcg_D_noalloc: needs more than the " + std::to_string(PCG_NOALLOC_SCRATCH_BYTES) +
+                         "-byte static scratch (x too large for the allocation-free path)");
+  int64_t wave_len = std::min<int64_t>({nseg, (int64_t) grid * 8,
+                                        (int64_t) ((PCG_NOALLOC_SCRATCH_BYTES - fixed) / per_row)});
+  int64_t* d_segsum = (int64_t*) (scratch + off);
+  off = align(off + (size_t) wave_len * 8);
+  uint32_t* d_cnt = (uint32_t*) (scratch + off);
+  off = align(off + (size_t) wave_len * cols * 4);
+  int32_t* d_smu = (int32_t*) (scratch + off);
+  off = align(off + (size_t) wave_len * cols * 4);
+  if (off > PCG_NOALLOC_SCRATCH_BYTES) fail(PCG_EINTERNAL, "no-alloc scratch carve overflow");
+
+  // everything that must start at zero
+  PCG_CUDA(cudaMemsetAsync(d_counters, 0, 4096, s));
+  PCG_CUDA(cudaMemsetAsync(d_run, 0, (size_t) cols * 8, s));
+  PCG_CUDA(cudaMemsetAsync(d_acc, 0, (size_t) cols * 16, s));
+  PCG_CUDA(cudaMemcpyAsync(d_xp, h_xp, (size_t) cols * 24, cudaMemcpyHostToDevice, s));
+  PCG_CUDA(cudaMemcpyAsync(d_seg, h_seg, (size_t) (nseg + 1) * 8, cudaMemcpyHostToDevice, s));
+
+  SweepArgs a;
+  memset(&a, 0, sizeof(a));
+  a.x_lo = (uint64_t) x;
+  a.x_hi = (uint64_t) (x >> 64);
+  a.y = pb.y;
+  a.z = pb.z;
+  a.k = pb.k;
+  a.L = L;
+  a.x_star = x_star;
+  a.seglo = d_seg;
+  a.words = words;
+  a.rec_cap = cap;
+  a.gourdon = 1;
+  a.pi_sqrt = (int) pi_sqrt;
+  a.bglob = (int) bglob;
+  a.primes = T.primes.as<uint32_t>();
+  a.nprimes = T.nprimes;
+  a.pitab = T.pitab.as<uint64_t>();
+  a.pi_max = T.prime_limit;
+  a.factor = T.factor_d.p;
+  a.xp_tab = d_xp;
+  a.coprime = T.coprime.as<uint16_t>();
+  a.cindex = T.cindex.as<int16_t>();
+  a.cnt = d_cnt;
+  a.smu = d_smu;
+  a.segsum = d_segsum;
+  a.counters = d_counters;
+  uint64_t launches = 0;
+  int waves = 0;
+  for (int64_t first = 0; first < nseg; first += wave_len) {
+    int wl = (int) std::min<int64_t>(wave_len, nseg - first);
+    a.wave_first = first;
+    a.wave_len = wl;
+    a.queue = d_queue + (waves % 16);
+    PCG_CUDA(cudaMemsetAsync(d_cnt, 0, (size_t) wl * cols * 4, s));
+    PCG_CUDA(cudaMemsetAsync(d_smu, 0, (size_t) wl * cols * 4, s));
+    if (waves % 16 == 0 && waves > 0) PCG_CUDA(cudaMemsetAsync(d_queue, 0, 64, s));
+    int g = (int) std::min<int64_t>(grid, wl);
+    if (fbytes == 2) launch_sweep<uint16_t, 256>(a, g, smem, s);
+    else launch_sweep<uint32_t, 256>(a, g, smem, s);
+    PCG_CUDA(cudaGetLastError());
+    k_combine<<<(cols + 255) / 256, 256, 0, s>>>(d_cnt, d_smu, wl, cols, d_run, d_acc);
+    k_segsum<<<1, 1024, 0, s>>>(d_segsum, wl, d_acc);
+    PCG_CUDA(cudaGetLastError());
+    launches += 3;
+    waves++;
+  }
+  unsigned long long ctr[4];
+  PCG_CUDA(cudaMemcpyAsync(h_acc, d_acc, (size_t) cols * 16, cudaMemcpyDeviceToHost, s));
+  PCG_CUDA(cudaMemcpyAsync(ctr, d_counters, sizeof(ctr), cudaMemcpyDeviceToHost, s));
+  PCG_CUDA(cudaStreamSynchronize(s));
+  i128 sum = 0;
+  for (int b = 0; b < cols; b++) sum += h_acc[b];
+  res.sum = sum;
+  st.leaves = ctr[0];
+  st.two_prime_leaves = ctr[1];
+  st.levels = ctr[2];
+  st.factor_entries = ctr[3];
+  st.segments = (uint64_t) nseg;
+  st.kernel_launches = launches;
+  st.sweep_launches = (uint64_t) waves;
+  st.h2d_bytes = (uint64_t) cols * 24 + (uint64_t) (nseg + 1) * 8;
+  st.d2h_bytes = (uint64_t) cols * 16 + sizeof(ctr);
   st.segment_words = words;
   st.ctas_per_sm = ctas;
   st.threads_per_cta = NT;

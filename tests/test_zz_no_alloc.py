@@ -1,0 +1,88 @@
+"""GPU: the allocation-free entry point pcg_D_noalloc against pcg_D.
+
+pcg_D_noalloc serves callers that cannot allocate device memory at the
+moment they need D(x, y, z, k): code running while a CUDA stream is being
+captured into a graph, a serving request path that must not touch the
+allocator, or a process whose device memory belongs to another framework's
+pool.  It reads the tables of a context built beforehand (set-up time, when
+allocating is allowed) and keeps all of its working memory in one static
+device array inside libpcgpu.so.
+
+This file sorts last so that, if it fails, a run stopping at the first
+failure has already run every other test.  It needs nothing from the other
+tests and passes alone in a fresh process.
+"""
+import ctypes
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _bind(pcg):
+    L = pcg.load()
+    L.pcg_D_noalloc.argtypes = [ctypes.c_void_p, pcg.I128, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                                ctypes.c_void_p, ctypes.POINTER(pcg.I128)]
+    L.pcg_D_noalloc.restype = ctypes.c_int
+    return L
+
+
+def _free_device_bytes():
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return torch.cuda.mem_get_info()[0]
+    except Exception:
+        pass
+    return None
+
+
+def test_noalloc_matches_pcg_D_on_two_calls(pcg):
+    L = _bind(pcg)
+    ctx = pcg.Context(10 ** 17)          # resident tables: built here, allocation allowed
+    try:
+        for x in (10 ** 12, 10 ** 14, 1234567890123456, 10 ** 17):
+            p = pcg.gourdon_params(x)
+            want = pcg.D(x, p["y"], p["z"], p["k"])          # the existing entry point
+            for _ in range(2):                                 # two calls in a row share the scratch
+                out = pcg.I128()
+                st = L.pcg_D_noalloc(ctx._h, pcg.to_i128(x), p["y"], p["z"], p["k"], None, ctypes.byref(out))
+                assert st == 0, L.pcg_last_error(ctx._h)
+                assert pcg.from_i128(out) == want, x           # integers: bit-exact
+    finally:
+        ctx.close()
+
+
+def test_noalloc_allocates_no_device_memory(pcg):
+    L = _bind(pcg)
+    ctx = pcg.Context(10 ** 16)
+    try:
+        x = 10 ** 16
+        p = pcg.gourdon_params(x)
+        out = pcg.I128()
+        # the first call on the device resolves the scratch address (and may
+        # load the module); the second one is measured
+        assert L.pcg_D_noalloc(ctx._h, pcg.to_i128(x), p["y"], p["z"], p["k"], None, ctypes.byref(out)) == 0
+        before = _free_device_bytes()
+        out2 = pcg.I128()
+        assert L.pcg_D_noalloc(ctx._h, pcg.to_i128(x), p["y"], p["z"], p["k"], None, ctypes.byref(out2)) == 0
+        after = _free_device_bytes()
+        assert pcg.from_i128(out2) == pcg.from_i128(out) == 257656447322004
+        if before is not None and after is not None:
+            assert abs(before - after) < (1 << 20)
+    finally:
+        ctx.close()
+
+
+def test_noalloc_rejects_uncovered_tables(pcg):
+    L = _bind(pcg)
+    ctx = pcg.Context(10 ** 12)
+    try:
+        x = 10 ** 16
+        p = pcg.gourdon_params(x)
+        out = pcg.I128()
+        st = L.pcg_D_noalloc(ctx._h, pcg.to_i128(x), p["y"], p["z"], p["k"], None, ctypes.byref(out))
+        assert st == 2  # PCG_ERANGE: the context's tables do not cover y, z
+        assert b"do not cover" in L.pcg_last_error(ctx._h)
+    finally:
+        ctx.close()
