@@ -151,6 +151,10 @@ pcg_status pcg_dr_params(pcg_i128 x, int64_t* y, int64_t* z, int64_t* c);
 
 /* pi(x), x < 2^127; -1 semantics are left to the primecount_* wrappers. */
 pcg_status pcg_pi(pcg_i128 x, const pcg_opts* opts, pcg_i128* out);
+/* The terms of Gourdon's formula for x > 1e10: out6 = {A + C, B, D, Phi0,
+ * Sigma, pi(x)} with pi = (A + C) - B + D + Phi0 + Sigma (the reference's
+ * --AC, --B, --D, --Phi0, --Sigma options, src/app/main.cpp:465-579). */
+pcg_status pcg_pi_terms(pcg_i128 x, const pcg_opts* opts, pcg_i128* out6);
 /* phi(x, a): numbers <= x not divisible by any of the first a primes. */
 pcg_status pcg_phi(int64_t x, int64_t a, const pcg_opts* opts, int64_t* out);
 

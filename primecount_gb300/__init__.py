@@ -88,6 +88,8 @@ def load(path=None):
     L.pcg_dr_params.argtypes = [I128, c_p(c_i64), c_p(c_i64), c_p(c_i64)]
     L.pcg_pi.argtypes = [I128, c_p(Opts), c_p(I128)]
     L.pcg_phi.argtypes = [c_i64, c_i64, c_p(Opts), c_p(c_i64)]
+    L.pcg_pi_terms.argtypes = [I128, c_p(Opts), c_p(I128)]
+    L.pcg_pi_terms.restype = ctypes.c_int
     L.pcg_pi_batch.argtypes = [c_p(I128), ctypes.c_size_t, c_p(I128), c_p(Opts)]
     L.pcg_phi_batch.argtypes = [c_p(c_i64), c_p(c_i64), ctypes.c_size_t, c_p(c_i64), c_p(Opts)]
     L.pcg_ctx_create.argtypes = [I128, ctypes.c_uint64, c_p(ctypes.c_void_p)]
@@ -218,6 +220,16 @@ def pi(x, threads=0, print=False, ctx=None, stream=None):
     o = _opts(ctx, stream, threads, print)
     _check(load().pcg_pi(to_i128(x), ctypes.byref(o), ctypes.byref(out)), ctx)
     return from_i128(out)
+
+
+def pi_terms(x, ctx=None, stream=None):
+    """The terms of Gourdon's formula for x > 1e10 (the reference's --AC, --B,
+    --D, --Phi0, --Sigma options): dict with AC, B, D, Phi0, Sigma and pi."""
+    out = (I128 * 6)()
+    o = _opts(ctx, stream)
+    _check(load().pcg_pi_terms(to_i128(x), ctypes.byref(o), out), ctx)
+    v = [from_i128(t) for t in out]
+    return dict(zip(("AC", "B", "D", "Phi0", "Sigma", "pi"), v))
 
 
 def phi(x, a, threads=0, ctx=None, stream=None):

@@ -240,6 +240,23 @@ static pcg_status guard(Ctx* c, F&& f)
   }
 }
 
+namespace pcg {
+pcg_status guarded_call(const pcg_opts* opts, void (*fn)(Ctx&, cudaStream_t, void*), void* arg)
+{
+  Ctx* cp = nullptr;
+  return guard(nullptr, [&] {
+    cp = ctx_from(opts);
+    cp->last_error.clear();
+    try {
+      fn(*cp, stream_from(*cp, opts), arg);
+    } catch (const Failure& e) {
+      cp->last_error = e.msg;
+      throw;
+    }
+  });
+}
+}  // namespace pcg
+
 static Tuning tuning_from(const pcg_opts* o)
 {
   Tuning t;

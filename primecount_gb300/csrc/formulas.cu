@@ -1,0 +1,989 @@
+// formulas.cu -- pi(x) by Gourdon's formula on the GPU, and phi(x, a).
+//
+// pi(x) = A - B + C + D + Phi0 + Sigma (reference: src/gourdon/pi_gourdon.cpp:
+// 37-163).  D comes from the hard-leaf sweep (sweep.cu); the easy terms are
+// evaluated here, each as the sum the reference's code computes, restated
+// over the whole interval instead of the reference's segments:
+//   A, C1, C2   src/gourdon/AC.cpp:40-300 (sums of pi(x / (p q)) and
+//               pi(x / (p q r)) over primes; the PiTable up to sqrt(x) lives
+//               in HBM and every (p, q) pair is one thread)
+//   B           src/gourdon/B.cpp:38-131 (sum of pi(x / p), y < p <= sqrt(x):
+//               a segmented prime sieve of [sqrt(x), x / y) whose segments
+//               are joined by the same offset scan as the hard leaves)
+//   Phi0        src/gourdon/Phi0.cpp:38-96 (mu(n) phi(x / n, k) over the
+//               FactorTableD entries)
+//   Sigma       src/gourdon/Sigma.cpp:25-140 (closed forms, on the host)
+// pi(x) for x <= 1e10 is a direct sieve count (the reference routes small x
+// to other algorithms, src/api.cpp:75-91).
+#include <cstdio>
+#include <cstring>
+#include <chrono>
+#include <algorithm>
+#include <vector>
+
+#include "pcg_internal.hpp"
+#include "dev_common.cuh"
+
+namespace pcg {
+
+static double fnow_ms()
+{
+  using namespace std::chrono;
+  return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+// ---------------------------------------------------------------- i128 block sums
+template <int NT>
+__device__ __forceinline__ void block_sum_i128(i128 v, i128* out)
+{
+  __shared__ long long lo_s[NT], hi_s[NT];
+  // split into 2^62-bounded halves so that a block of partial sums cannot overflow
+  lo_s[threadIdx.x] = (long long) (v & (i128) 0x3FFFFFFFFFFFFFFFll);
+  hi_s[threadIdx.x] = (long long) (v >> 62);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    i128 lo = 0, hi = 0;
+    for (int i = 0; i < NT; i++) { lo += lo_s[i]; hi += hi_s[i]; }
+    *out += lo + hi * ((i128) 1 << 62);
+  }
+  __syncthreads();
+}
+
+static i128 sum_partials(const DevBuf& buf, int n, cudaStream_t s)
+{
+  std::vector<i128> h((size_t) n);
+  PCG_CUDA(cudaMemcpyAsync(h.data(), buf.p, (size_t) n * 16, cudaMemcpyDeviceToHost, s));
+  PCG_CUDA(cudaStreamSynchronize(s));
+  i128 t = 0;
+  for (int i = 0; i < n; i++) t += h[(size_t) i];
+  return t;
+}
+
+// ---------------------------------------------------------------- phi(v, k), k <= 8
+// phi(v, k) = (v / P) * phi(P) + phi(v mod P, k), P = p_1 ... p_k
+// (the identity of the reference's PhiTiny, src/PhiTiny.hpp:2-12); phi(r, k)
+// for r < P from a bitmap of the numbers coprime to p_1..p_k.
+__global__ void k_phi_bits(uint64_t* __restrict__ bits, uint32_t* __restrict__ pc, int64_t nwords, uint64_t P, int k)
+{
+  int64_t w = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nwords) return;
+  const uint32_t pr[8] = {2, 3, 5, 7, 11, 13, 17, 19};
+  uint64_t v = 0;
+  for (int j = 0; j < 64; j++) {
+    uint64_t t = 64 * (uint64_t) w + j;
+    if (t >= P) break;
+    bool ok = true;
+    for (int i = 0; i < k; i++) ok = ok && (t % pr[i] != 0);
+    if (ok) v |= 1ull << j;
+  }
+  bits[w] = v;
+  pc[w] = __popcll(v);
+}
+
+struct PhiTab {
+  const uint64_t* bits;
+  const uint64_t* pref;
+  uint64_t P, tot;
+  int k;
+};
+
+__device__ __forceinline__ i128 dphi_tiny(u128 v, const PhiTab& T)
+{
+  if (T.k == 0) return (i128) v;
+  const u128 q = div128(v, T.P);
+  const uint64_t r = (uint64_t) (v - q * T.P);
+  const uint64_t w = r >> 6;
+  const uint64_t c = T.pref[w] + __popcll(T.bits[w] & ((2ull << (r & 63)) - 1));
+  return (i128) q * (i128) T.tot + (i128) c;
+}
+
+static void ensure_phi_tiny(Ctx& c, int k, cudaStream_t s)
+{
+  Tables& t = c.tab;
+  if (t.phik == k) return;
+  static const uint64_t pr[8] = {2, 3, 5, 7, 11, 13, 17, 19};
+  uint64_t P = 1, tot = 1;
+  for (int i = 0; i < k; i++) { P *= pr[i]; tot *= pr[i] - 1; }
+  int64_t nwords = (int64_t) ((P + 63) / 64);
+  t.phi_bits.alloc((size_t) nwords * 8);
+  t.phi_pref.alloc((size_t) nwords * 8);
+  DevBuf pc;
+  pc.alloc((size_t) nwords * 4);
+  k_phi_bits<<<(unsigned) ((nwords + 255) / 256), 256, 0, s>>>(t.phi_bits.as<uint64_t>(), pc.as<uint32_t>(), nwords, P, k);
+  PCG_CUDA(cudaGetLastError());
+  exclusive_scan_u32(pc.as<uint32_t>(), nwords, t.phi_pref.as<uint64_t>(), s);
+  t.phik = k;
+  t.phi_P = P;
+  t.phi_tot = tot;
+}
+
+static PhiTab phi_tab(const Ctx& c)
+{
+  PhiTab T;
+  T.bits = c.tab.phi_bits.as<uint64_t>();
+  T.pref = c.tab.phi_pref.as<uint64_t>();
+  T.P = c.tab.phi_P;
+  T.tot = c.tab.phi_tot;
+  T.k = c.tab.phik;
+  return T;
+}
+
+// ---------------------------------------------------------------- Phi0
+// Phi0 = sum over n = 1 and the square-free n <= z whose prime factors lie
+// in (p_k, y] of mu(n) phi(x / n, k) (Phi0.cpp:38-96).  Those n are the
+// FactorTableD entries above 2k + 1 (1 -> T_MAX - 1, composites 2 pi(lpf) +
+// [mu = -1]) except the primes <= p_k, which the table marks T_MAX like every
+// prime <= y.
+template <typename FT>
+__global__ void __launch_bounds__(256) k_phi0(uint64_t x_lo, uint64_t x_hi, const FT* __restrict__ factor,
+                                              int64_t size, uint32_t thr, uint64_t pk, PhiTab T,
+                                              const uint16_t* __restrict__ coprime, i128* __restrict__ partial)
+{
+  const u128 x = ((u128) x_hi << 64) | x_lo;
+  i128 acc = 0;
+  for (int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x; i < size; i += (int64_t) gridDim.x * blockDim.x) {
+    const uint32_t f = (uint32_t) factor[i];
+    if (f > thr) {
+      const uint64_t n = 2310 * (uint64_t) (i / 480) + coprime[i % 480];
+      if (n > 1 && n <= pk) continue;
+      const i128 t = dphi_tiny(div128(x, n), T);
+      acc += (f & 1) ? -t : t;
+    }
+  }
+  block_sum_i128<256>(acc, &partial[blockIdx.x]);
+}
+
+// ---------------------------------------------------------------- A and C
+// One outer item: a prime p_b (or p_b q for the C1 products) and a range
+// (i_lo, i_hi] of prime indices q = primes[i]; the term of q is
+//   mode 0 (A):  w * pi(xp / q), w = 1 if q <= cap else 2   (AC.cpp:40-83)
+//   mode 1 (C):  pi(xp / q) - b + 2                         (AC.cpp:112-129, 186-300)
+//   mode 2 (C1 products): -(pi(xp / q) - b + 2)              (AC.cpp:131-177)
+//   mode 3 (P3 of phi):   pi(xp / q) - i + 1, i = index of q
+struct PairOuter {
+  uint64_t xp_lo, xp_hi;
+  uint64_t cap;
+  int64_t i_lo, i_hi;
+  int32_t b;
+  int32_t mode;
+};
+
+__global__ void __launch_bounds__(256) k_pairs(const PairOuter* __restrict__ outs, int64_t n_outer,
+                                               const uint32_t* __restrict__ primes,
+                                               const uint64_t* __restrict__ pibig, i128* __restrict__ partial)
+{
+  i128 acc = 0;
+  for (int64_t o = blockIdx.x; o < n_outer; o += gridDim.x) {
+    const PairOuter O = outs[o];
+    long long s = 0;
+    for (int64_t i = O.i_lo + 1 + threadIdx.x; i <= O.i_hi; i += blockDim.x) {
+      const uint64_t q = primes[i];
+      uint64_t n;
+      if (O.xp_hi == 0) n = O.xp_lo / q;
+      else n = (uint64_t) ((((u128) O.xp_hi << 64) | O.xp_lo) / q);
+      const long long pin = dpi(pibig, n);
+      if (O.mode == 0) s += (q <= O.cap) ? pin : 2 * pin;
+      else if (O.mode == 1) s += pin - O.b + 2;
+      else if (O.mode == 2) s -= pin - O.b + 2;
+      else s += pin - i + 1;
+    }
+    acc += s;
+  }
+  block_sum_i128<256>(acc, &partial[blockIdx.x]);
+}
+
+struct AcParams {
+  uint64_t x_lo, x_hi;
+  int64_t y, z, k, x_star, x13, sqrtx;
+  int64_t bA0, bA1;      // A:  b in (bA0, bA1]
+  int64_t bC10, bC11;    // C1: b in (bC10, bC11]
+  int64_t bC20, bC21;    // C2: b in (bC20, bC21]
+  const uint32_t* primes;
+  const uint64_t* pismall;  // PiTable up to y
+  const uint64_t* pibig;    // PiTable up to sqrt(x)
+};
+
+// A outers: b in (pi(x*), pi(x^(1/3))], q in (max(p, xp / sqrt(x)), sqrt(xp)]
+__global__ void k_outer_A(AcParams P, PairOuter* __restrict__ outs)
+{
+  const int64_t j = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t b = P.bA0 + 1 + j;
+  if (b > P.bA1) return;
+  const u128 x = ((u128) P.x_hi << 64) | P.x_lo;
+  const uint64_t p = P.primes[b];
+  const u128 xp = div128(x, p);
+  PairOuter O;
+  O.xp_lo = (uint64_t) xp;
+  O.xp_hi = (uint64_t) (xp >> 64);
+  O.cap = (uint64_t) (xp / (u128) P.y);
+  O.b = (int32_t) b;
+  O.mode = 0;
+  const int64_t sq = disqrt(xp);
+  const int64_t lowq = (int64_t) (xp / (u128) P.sqrtx);
+  O.i_hi = dpi(P.pibig, (uint64_t) sq);
+  O.i_lo = dmax(b, dpi(P.pibig, (uint64_t) lowq));
+  if (O.i_hi < O.i_lo) O.i_hi = O.i_lo;
+  outs[j] = O;
+}
+
+// the m-range of C1 for p_b: (max(x / p^3, z / p), min(x / p, z)]
+__device__ __forceinline__ void c1_range(const AcParams& P, int64_t b, u128& xp, int64_t& min_m, int64_t& max_m)
+{
+  const u128 x = ((u128) P.x_hi << 64) | P.x_lo;
+  const uint64_t p = P.primes[b];
+  xp = div128(x, p);
+  max_m = (xp < (u128) P.z) ? (int64_t) xp : P.z;
+  const u128 xpp = xp / ((u128) p * p);
+  min_m = dmax(xpp > (u128) INT64_MAX ? INT64_MAX : (int64_t) xpp, P.z / (int64_t) p);
+}
+
+// C1 outers with m prime: primes m in (min_m, min(y, max_m)]
+__global__ void k_outer_C1(AcParams P, PairOuter* __restrict__ outs)
+{
+  const int64_t j = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t b = P.bC10 + 1 + j;
+  if (b > P.bC11) return;
+  u128 xp;
+  int64_t min_m, max_m;
+  c1_range(P, b, xp, min_m, max_m);
+  PairOuter O;
+  O.xp_lo = (uint64_t) xp;
+  O.xp_hi = (uint64_t) (xp >> 64);
+  O.cap = 0;
+  O.b = (int32_t) b;
+  O.mode = 1;
+  O.i_lo = O.i_hi = 0;
+  const int64_t top = dmin(P.y, max_m);
+  if (min_m < max_m && min_m < top) {
+    O.i_lo = dpi(P.pismall, (uint64_t) min_m);
+    O.i_hi = dpi(P.pismall, (uint64_t) top);
+  }
+  outs[j] = O;
+}
+
+// C1 products m = q r: number of q per b, then one outer per (b, q)
+__global__ void k_c1_qcount(AcParams P, int64_t* __restrict__ qlo, int64_t* __restrict__ qcnt)
+{
+  const int64_t j = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t b = P.bC10 + 1 + j;
+  if (b > P.bC11) return;
+  u128 xp;
+  int64_t min_m, max_m;
+  c1_range(P, b, xp, min_m, max_m);
+  const int64_t p = P.primes[b];
+  int64_t lo = 0, cnt = 0;
+  if (min_m < max_m) {
+    const int64_t max_q = dmin(P.y, disqrt((u128) max_m));
+    const int64_t min_q = dmax(p, min_m / P.y);
+    if (min_q < max_q) {
+      lo = dpi(P.pismall, (uint64_t) min_q);
+      cnt = dpi(P.pismall, (uint64_t) max_q) - lo;
+    }
+  }
+  qlo[j] = lo;
+  qcnt[j] = cnt;
+}
+
+__global__ void k_c1_expand(AcParams P, const int64_t* __restrict__ qlo, const int64_t* __restrict__ qcnt,
+                            const int64_t* __restrict__ qoff, PairOuter* __restrict__ outs)
+{
+  const int64_t j = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t b = P.bC10 + 1 + j;
+  if (b > P.bC11) return;
+  u128 xp;
+  int64_t min_m, max_m;
+  c1_range(P, b, xp, min_m, max_m);
+  for (int64_t t = 0; t < qcnt[j]; t++) {
+    const int64_t qi = qlo[j] + 1 + t;
+    const uint64_t q = P.primes[qi];
+    const int64_t min_r = dmax((int64_t) q, min_m / (int64_t) q);
+    const int64_t max_r = dmin(P.y, max_m / (int64_t) q);
+    PairOuter O;
+    const u128 xpq = div128(xp, q);
+    O.xp_lo = (uint64_t) xpq;
+    O.xp_hi = (uint64_t) (xpq >> 64);
+    O.cap = 0;
+    O.b = (int32_t) b;
+    O.mode = 2;
+    O.i_lo = O.i_hi = 0;
+    if (min_r < max_r) {
+      O.i_lo = dpi(P.pismall, (uint64_t) min_r);
+      O.i_hi = dpi(P.pismall, (uint64_t) max_r);
+    }
+    outs[qoff[j] + t] = O;
+  }
+}
+
+// C2 outers: primes q in (max(x / p^3, p, xp / sqrt(x)), min(x / p^2, y)]
+__global__ void k_outer_C2(AcParams P, PairOuter* __restrict__ outs)
+{
+  const int64_t j = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t b = P.bC20 + 1 + j;
+  if (b > P.bC21) return;
+  const u128 x = ((u128) P.x_hi << 64) | P.x_lo;
+  const uint64_t p = P.primes[b];
+  const u128 xp = div128(x, p);
+  const u128 xpp = xp / (u128) p;
+  const int64_t max_m = (xpp < (u128) P.y) ? (int64_t) xpp : P.y;
+  const u128 x3 = xp / ((u128) p * p);
+  int64_t min_m = x3 > (u128) INT64_MAX ? INT64_MAX : (int64_t) x3;
+  min_m = dmax(min_m, (int64_t) p);
+  min_m = dmax(min_m, (int64_t) (xp / (u128) P.sqrtx));
+  PairOuter O;
+  O.xp_lo = (uint64_t) xp;
+  O.xp_hi = (uint64_t) (xp >> 64);
+  O.cap = 0;
+  O.b = (int32_t) b;
+  O.mode = 1;
+  O.i_lo = O.i_hi = 0;
+  if (min_m < max_m) {
+    O.i_lo = dpi(P.pismall, (uint64_t) min_m);
+    O.i_hi = dpi(P.pismall, (uint64_t) max_m);
+  }
+  outs[j] = O;
+}
+
+// ---------------------------------------------------------------- prime sieve segments (B, small pi)
+// Each CTA sieves a segment [lo, hi) (lo a multiple of 240) of the numbers
+// coprime to 30 with every prime 7 <= p <= sqrt(hi), leaving the primes.
+// Mode count: seg_c[s] = # primes >= 7 in the segment.  Mode B additionally
+// answers the queries x / p for the primes p in (max(y, x / hi), min(sqrt(x),
+// x / lo)] (enumerated from the PiTable bits up to sqrt(x)): seg_m[s] = # of
+// them, seg_l[s] = sum of # primes in [lo, x / p].
+#define PS_WORDS 16384
+#define PS_NT 512
+struct PsArgs {
+  uint64_t x_lo, x_hi;
+  int64_t lo0;           // first segment start (multiple of 240)
+  int64_t end;           // sieve [lo0, end)
+  int64_t seg;           // numbers per segment = PS_WORDS * 240
+  int64_t nseg;
+  int64_t qlo, qhi;      // B queries: primes p in (qlo, qhi]
+  int32_t mode;          // 0 count, 1 B
+  int32_t nbase;
+  const uint32_t* base;  // primes >= 7 up to sqrt(end)
+  const uint64_t* pibig; // PiTable bits for the B queries
+  int64_t* seg_c;
+  int64_t* seg_m;
+  int64_t* seg_l;
+  int* queue;
+};
+
+__global__ void __launch_bounds__(PS_NT) k_psieve(const PsArgs A)
+{
+  extern __shared__ __align__(16) unsigned char psm[];
+  uint64_t* bits = (uint64_t*) psm;
+  uint32_t* pref = (uint32_t*) (bits + PS_WORDS);       // PS_WORDS / 8 chunk prefixes
+  __shared__ int s_s;
+  __shared__ uint32_t wt[32];
+  __shared__ long long red[3][32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nch = PS_WORDS / 8;
+  const u128 x = ((u128) A.x_hi << 64) | A.x_lo;
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) s_s = atomicAdd(A.queue, 1);
+    __syncthreads();
+    const int64_t s = s_s;
+    if (s >= A.nseg) break;
+    const uint64_t lo = (uint64_t) (A.lo0 + s * A.seg);
+    const uint64_t hi = (uint64_t) dmin((int64_t) lo + A.seg, A.end);
+    const uint32_t span = (uint32_t) (hi - lo);
+    const int wused = (int) ((span + 239) / 240);
+    for (int w = tid; w < PS_WORDS; w += PS_NT) {
+      uint64_t v = w < wused ? ~0ull : 0ull;
+      if (w == wused - 1) v &= mask_le((span - 1) % 240);
+      if (lo == 0 && w == 0) v &= ~1ull;        // 1 is not prime
+      bits[w] = v;
+    }
+    __syncthreads();
+    // cross off p * q, q >= p, q coprime to 30: a warp per prime for small p,
+    // a lane per prime for large ones
+    for (int k = warp; k < A.nbase; k += PS_NT / 32) {
+      const uint64_t p = A.base[k];
+      if (p * p >= hi) break;
+      if (p >= 4096) break;
+      uint64_t qlo = (lo + p - 1) / p;
+      if (qlo < p) qlo = p;
+      const uint64_t qhi = (hi - 1) / p;
+      if (qlo > qhi) continue;
+      const uint64_t jlo = cnt_le(qlo - 1), jhi = cnt_le(qhi);
+      for (uint64_t j = jlo + lane; j < jhi; j += 32) {
+        const uint64_t q = 30 * (j >> 3) + woff((uint32_t) (j & 7));
+        const uint32_t off = (uint32_t) (p * q - lo);
+        const uint32_t w = off / 240, r = off - w * 240;
+        atomicAnd((unsigned long long*) &bits[w], ~(1ull << bit_of(r)));
+      }
+    }
+    for (int k = tid; k < A.nbase; k += PS_NT) {
+      const uint64_t p = A.base[k];
+      if (p < 4096) continue;
+      if (p * p >= hi) break;
+      uint64_t qlo = (lo + p - 1) / p;
+      if (qlo < p) qlo = p;
+      const uint64_t qhi = (hi - 1) / p;
+      if (qlo > qhi) continue;
+      const uint64_t jlo = cnt_le(qlo - 1), jhi = cnt_le(qhi);
+      for (uint64_t j = jlo; j < jhi; j++) {
+        const uint64_t q = 30 * (j >> 3) + woff((uint32_t) (j & 7));
+        const uint32_t off = (uint32_t) (p * q - lo);
+        const uint32_t w = off / 240, r = off - w * 240;
+        atomicAnd((unsigned long long*) &bits[w], ~(1ull << bit_of(r)));
+      }
+    }
+    __syncthreads();
+    // chunk prefix (8 words per chunk; nch / PS_NT chunks per thread)
+    {
+      const int cpt = nch / PS_NT;
+      const int base = tid * cpt;
+      uint32_t loc[4];
+      uint32_t sum = 0;
+      for (int c = 0; c < cpt; c++) {
+        uint32_t t = 0;
+        for (int i = 0; i < 8; i++) t += __popcll(bits[8 * (base + c) + i]);
+        loc[c] = t;
+        sum += t;
+      }
+      uint32_t incl = sum;
+      for (int d = 1; d < 32; d <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += t;
+      }
+      if (lane == 31) wt[warp] = incl;
+      __syncthreads();
+      uint32_t run = incl - sum;
+      for (int w = 0; w < warp; w++) run += wt[w];
+      for (int c = 0; c < cpt; c++) { pref[base + c] = run; run += loc[c]; }
+      if (tid == PS_NT - 1 && A.seg_c) A.seg_c[s] = run;
+      __syncthreads();
+    }
+    if (A.mode == 1) {
+      // primes p with x / p in [lo, hi): p in (x / hi, x / lo], inside (qlo, qhi]
+      const int64_t pa = dmax(A.qlo, (int64_t) div128(x, hi));
+      const int64_t pb = (lo == 0) ? A.qhi : dmin(A.qhi, (int64_t) div128(x, lo));
+      long long lsum = 0, cnt = 0;
+      if (pb > pa) {
+        const int64_t w0 = (pa + 1) / 240, w1 = pb / 240;
+        for (int64_t w = w0 + tid; w <= w1; w += PS_NT) {
+          uint64_t bw = A.pibig[2 * w + 1];
+          while (bw) {
+            const int j = __ffsll((long long) bw) - 1;
+            bw &= bw - 1;
+            const int64_t p = 240 * w + 30 * (j >> 3) + woff(j & 7);
+            if (p <= pa || p > pb) continue;
+            const uint64_t n = (uint64_t) div128(x, (uint64_t) p);
+            const uint32_t off = (uint32_t) (n - lo);
+            const uint32_t ww = off / 240, r = off - ww * 240;
+            uint32_t v = pref[ww >> 3];
+            for (uint32_t i = ww & ~7u; i < ww; i++) v += __popcll(bits[i]);
+            v += __popcll(bits[ww] & mask_le(r));
+            lsum += v;
+            cnt++;
+          }
+        }
+      }
+      for (int d = 16; d > 0; d >>= 1) {
+        lsum += __shfl_down_sync(0xffffffffu, lsum, d);
+        cnt += __shfl_down_sync(0xffffffffu, cnt, d);
+      }
+      if (lane == 0) { red[0][warp] = lsum; red[1][warp] = cnt; }
+      __syncthreads();
+      if (tid == 0) {
+        long long a = 0, b = 0;
+        for (int i = 0; i < PS_NT / 32; i++) { a += red[0][i]; b += red[1][i]; }
+        A.seg_l[s] = a;
+        A.seg_m[s] = b;
+      }
+    }
+  }
+}
+
+static std::vector<uint32_t> base_primes7(int64_t limit)
+{
+  std::vector<uint8_t> c((size_t) limit + 1, 0);
+  std::vector<uint32_t> p;
+  for (int64_t i = 2; i <= limit; i++) {
+    if (c[(size_t) i]) continue;
+    if (i >= 7) p.push_back((uint32_t) i);
+    for (int64_t m = i * i; m <= limit; m += i) c[(size_t) m] = 1;
+  }
+  return p;
+}
+
+struct PsOut {
+  std::vector<int64_t> c, m, l;
+  int64_t lo0 = 0, nseg = 0;
+};
+
+// sieve [lo0, end) in segments; B queries for primes in (qlo, qhi] when b_mode
+static PsOut run_psieve(Ctx& c, u128 x, int64_t lo0, int64_t end, bool b_mode, int64_t qlo, int64_t qhi,
+                        cudaStream_t s, uint64_t* launches)
+{
+  PsOut o;
+  lo0 -= lo0 % 240;
+  o.lo0 = lo0;
+  const int64_t seg = (int64_t) PS_WORDS * 240;
+  o.nseg = (end - lo0 + seg - 1) / seg;
+  if (o.nseg <= 0) return o;
+  std::vector<uint32_t> base = base_primes7(isqrt((u128) end) + 1);
+  DevBuf d_base, d_c, d_m, d_l, d_q;
+  d_base.alloc(std::max<size_t>(base.size(), 1) * 4);
+  d_c.alloc((size_t) o.nseg * 8);
+  d_m.alloc((size_t) o.nseg * 8);
+  d_l.alloc((size_t) o.nseg * 8);
+  d_q.alloc(64);
+  if (!base.empty()) PCG_CUDA(cudaMemcpyAsync(d_base.p, base.data(), base.size() * 4, cudaMemcpyHostToDevice, s));
+  PCG_CUDA(cudaMemsetAsync(d_q.p, 0, 64, s));
+  PCG_CUDA(cudaMemsetAsync(d_m.p, 0, (size_t) o.nseg * 8, s));
+  PCG_CUDA(cudaMemsetAsync(d_l.p, 0, (size_t) o.nseg * 8, s));
+  PsArgs a;
+  memset(&a, 0, sizeof(a));
+  a.x_lo = (uint64_t) x;
+  a.x_hi = (uint64_t) (x >> 64);
+  a.lo0 = lo0;
+  a.end = end;
+  a.seg = seg;
+  a.nseg = o.nseg;
+  a.qlo = qlo;
+  a.qhi = qhi;
+  a.mode = b_mode ? 1 : 0;
+  a.nbase = (int) base.size();
+  a.base = d_base.as<uint32_t>();
+  a.pibig = c.tab.pibig.as<uint64_t>();
+  a.seg_c = d_c.as<int64_t>();
+  a.seg_m = d_m.as<int64_t>();
+  a.seg_l = d_l.as<int64_t>();
+  a.queue = d_q.as<int>();
+  const size_t smem = (size_t) PS_WORDS * 8 + (PS_WORDS / 8) * 4;
+  static bool attr = false;
+  if (!attr) {
+    PCG_CUDA(cudaFuncSetAttribute(k_psieve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
+    attr = true;
+  }
+  int occ = 0;
+  PCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_psieve, PS_NT, smem));
+  const int grid = (int) std::min<int64_t>((int64_t) c.num_sms * std::max(occ, 1), o.nseg);
+  k_psieve<<<grid, PS_NT, smem, s>>>(a);
+  PCG_CUDA(cudaGetLastError());
+  if (launches) *launches += 1;
+  o.c.resize((size_t) o.nseg);
+  o.m.resize((size_t) o.nseg);
+  o.l.resize((size_t) o.nseg);
+  PCG_CUDA(cudaMemcpyAsync(o.c.data(), d_c.p, (size_t) o.nseg * 8, cudaMemcpyDeviceToHost, s));
+  PCG_CUDA(cudaMemcpyAsync(o.m.data(), d_m.p, (size_t) o.nseg * 8, cudaMemcpyDeviceToHost, s));
+  PCG_CUDA(cudaMemcpyAsync(o.l.data(), d_l.p, (size_t) o.nseg * 8, cudaMemcpyDeviceToHost, s));
+  PCG_CUDA(cudaStreamSynchronize(s));
+  return o;
+}
+
+// pi(x) for small x: a direct sieve count (2, 3, 5 are not in the bitmap)
+static i128 pi_sieve_count(Ctx& c, int64_t x, cudaStream_t s, uint64_t* launches)
+{
+  if (x < 2) return 0;
+  if (x < 7) return x >= 5 ? 3 : (x >= 3 ? 2 : 1);
+  PsOut o = run_psieve(c, (u128) x, 0, x + 1, false, 0, 0, s, launches);
+  i128 t = 3;
+  for (int64_t i = 0; i < o.nseg; i++) t += o.c[(size_t) i];
+  return t;
+}
+
+// device pi lookups of a batch of values in the PiTable up to sqrt(x)
+__global__ void k_pi_lookup(const uint64_t* __restrict__ pt, const uint64_t* __restrict__ v, int64_t n,
+                            int64_t* __restrict__ out)
+{
+  int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = dpi(pt, v[i]);
+}
+
+static std::vector<int64_t> pi_lookup(Ctx& c, const std::vector<uint64_t>& v, cudaStream_t s)
+{
+  std::vector<int64_t> r(v.size());
+  if (v.empty()) return r;
+  for (uint64_t t : v)
+    if ((int64_t) t < 0 || (int64_t) t > c.tab.pibig_limit) fail(PCG_EINTERNAL, "pi lookup beyond the PiTable");
+  DevBuf dv, dr;
+  dv.alloc(v.size() * 8);
+  dr.alloc(v.size() * 8);
+  PCG_CUDA(cudaMemcpyAsync(dv.p, v.data(), v.size() * 8, cudaMemcpyHostToDevice, s));
+  k_pi_lookup<<<(unsigned) ((v.size() + 255) / 256), 256, 0, s>>>(c.tab.pibig.as<uint64_t>(), dv.as<uint64_t>(),
+                                                                   (int64_t) v.size(), dr.as<int64_t>());
+  PCG_CUDA(cudaGetLastError());
+  PCG_CUDA(cudaMemcpyAsync(r.data(), dr.p, v.size() * 8, cudaMemcpyDeviceToHost, s));
+  PCG_CUDA(cudaStreamSynchronize(s));
+  return r;
+}
+
+// ---------------------------------------------------------------- pi(x), Gourdon
+struct PiParts {
+  i128 ac = 0, b = 0, d = 0, phi0 = 0, sigma = 0, pi = 0;
+  double ms_d = 0, ms_ac = 0, ms_b = 0, ms_phi0 = 0, ms_sigma = 0, ms_tables = 0;
+  uint64_t launches = 0;
+  pcg_stats dstats{};
+};
+
+static void ensure_pibig(Ctx& c, int64_t limit, cudaStream_t s)
+{
+  if (c.tab.pibig_limit >= limit) return;
+  build_pitab_only(c.tab.pibig, limit, s);
+  c.tab.pibig_limit = limit;
+}
+
+static PiParts pi_gourdon(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s)
+{
+  PiParts R;
+  GourdonParams g = gourdon_params(x);
+  const int64_t y = g.y, z = g.z, k = g.k, x_star = g.x_star;
+  if (x > ((u128) y << 62)) fail(PCG_ERANGE, "pi_gourdon(x): x is too large");
+  const int64_t sqrtx = isqrt(x);
+  const int64_t x13 = iroot(x, 3);
+  double t0 = fnow_ms();
+  ensure_prime_tables(c, std::max<int64_t>(y, sqrtx > 0 ? std::min<int64_t>(y, sqrtx) : y), s);
+  ensure_factor_d(c, y, z, s);
+  ensure_pibig(c, sqrtx + 240, s);
+  ensure_phi_tiny(c, (int) k, s);
+  R.ms_tables = fnow_ms() - t0;
+  const Tables& T = c.tab;
+
+  // ---- D (hard special leaves)
+  {
+    double t1 = fnow_ms();
+    SweepProblem p;
+    p.gourdon = 1;
+    p.x = x;
+    p.y = y;
+    p.z = z;
+    p.k = k;
+    SweepResult r = run_sweep(c, p, tune, s);
+    R.d = r.sum;
+    R.dstats = r.stats;
+    R.launches += r.stats.kernel_launches;
+    R.ms_d = fnow_ms() - t1;
+  }
+
+  // ---- A + C
+  {
+    double t1 = fnow_ms();
+    const u128 xy = x / (u128) y, xz = x / (u128) z;
+    AcParams P;
+    memset(&P, 0, sizeof(P));
+    P.x_lo = (uint64_t) x;
+    P.x_hi = (uint64_t) (x >> 64);
+    P.y = y;
+    P.z = z;
+    P.k = k;
+    P.x_star = x_star;
+    P.x13 = x13;
+    P.sqrtx = sqrtx;
+    P.primes = T.primes.as<uint32_t>();
+    P.pismall = T.pitab.as<uint64_t>();
+    P.pibig = T.pibig.as<uint64_t>();
+    const int64_t pi_sqrtz = host_pi(T, (uint64_t) isqrt((u128) z));
+    P.bA0 = host_pi(T, (uint64_t) x_star);
+    P.bA1 = host_pi(T, (uint64_t) x13);
+    P.bC10 = std::max<int64_t>(k, host_pi(T, (uint64_t) iroot(xz, 3)));
+    P.bC11 = pi_sqrtz;
+    P.bC20 = std::max<int64_t>({k, host_pi(T, (uint64_t) iroot(xy, 3)), pi_sqrtz});
+    P.bC21 = host_pi(T, (uint64_t) x_star);
+    const int64_t nA = std::max<int64_t>(0, P.bA1 - P.bA0);
+    const int64_t nC1 = std::max<int64_t>(0, P.bC11 - P.bC10);
+    const int64_t nC2 = std::max<int64_t>(0, P.bC21 - P.bC20);
+    // C1 products: count q per b, then expand
+    int64_t nQ = 0;
+    DevBuf qlo, qcnt, qoff;
+    std::vector<int64_t> hq;
+    if (nC1 > 0) {
+      qlo.alloc((size_t) nC1 * 8);
+      qcnt.alloc((size_t) nC1 * 8);
+      qoff.alloc((size_t) nC1 * 8);
+      k_c1_qcount<<<(unsigned) ((nC1 + 127) / 128), 128, 0, s>>>(P, qlo.as<int64_t>(), qcnt.as<int64_t>());
+      PCG_CUDA(cudaGetLastError());
+      R.launches++;
+      hq.resize((size_t) nC1);
+      PCG_CUDA(cudaMemcpyAsync(hq.data(), qcnt.p, (size_t) nC1 * 8, cudaMemcpyDeviceToHost, s));
+      PCG_CUDA(cudaStreamSynchronize(s));
+      std::vector<int64_t> off((size_t) nC1);
+      for (int64_t j = 0; j < nC1; j++) { off[(size_t) j] = nQ; nQ += hq[(size_t) j]; }
+      PCG_CUDA(cudaMemcpyAsync(qoff.p, off.data(), (size_t) nC1 * 8, cudaMemcpyHostToDevice, s));
+    }
+    const int64_t nout = nA + nC1 + nQ + nC2;
+    i128 sum = 0;
+    if (nout > 0) {
+      DevBuf outs;
+      outs.alloc((size_t) nout * sizeof(PairOuter));
+      PairOuter* o = outs.as<PairOuter>();
+      if (nA) k_outer_A<<<(unsigned) ((nA + 127) / 128), 128, 0, s>>>(P, o);
+      if (nC1) k_outer_C1<<<(unsigned) ((nC1 + 127) / 128), 128, 0, s>>>(P, o + nA);
+      if (nQ) k_c1_expand<<<(unsigned) ((nC1 + 127) / 128), 128, 0, s>>>(P, qlo.as<int64_t>(), qcnt.as<int64_t>(),
+                                                                          qoff.as<int64_t>(), o + nA + nC1);
+      if (nC2) k_outer_C2<<<(unsigned) ((nC2 + 127) / 128), 128, 0, s>>>(P, o + nA + nC1 + nQ);
+      PCG_CUDA(cudaGetLastError());
+      R.launches += 4;
+      const int grid = (int) std::min<int64_t>(nout, (int64_t) c.num_sms * 8);
+      DevBuf part;
+      part.alloc((size_t) grid * 16);
+      PCG_CUDA(cudaMemsetAsync(part.p, 0, (size_t) grid * 16, s));
+      k_pairs<<<grid, 256, 0, s>>>(o, nout, T.primes.as<uint32_t>(), T.pibig.as<uint64_t>(), part.as<i128>());
+      PCG_CUDA(cudaGetLastError());
+      R.launches++;
+      sum = sum_partials(part, grid, s);
+    }
+    R.ac = sum;
+    R.ms_ac = fnow_ms() - t1;
+  }
+
+  // ---- B = sum over primes y < p <= sqrt(x) of pi(x / p)
+  {
+    double t1 = fnow_ms();
+    const int64_t n0 = (int64_t) (x / (u128) sqrtx);   // smallest x / p
+    const int64_t n1 = (int64_t) (x / (u128) (y + 1)) + 1;  // x / p < n1 for p > y
+    i128 B = 0;
+    if (sqrtx > y && n1 > n0) {
+      PsOut o = run_psieve(c, x, n0, n1, true, y, sqrtx, s, &R.launches);
+      // pi(lo0 - 1) from the PiTable up to sqrt(x) (lo0 >= sqrt(x) > 1e5 here)
+      i128 run = 0;
+      if (o.lo0 >= 7) run = pi_lookup(c, std::vector<uint64_t>{(uint64_t) (o.lo0 - 1)}, s)[0];
+      for (int64_t i = 0; i < o.nseg; i++) {
+        B += (i128) o.l[(size_t) i] + (i128) o.m[(size_t) i] * run;
+        run += o.c[(size_t) i];
+      }
+    }
+    R.b = B;
+    R.ms_b = fnow_ms() - t1;
+  }
+
+  // ---- Phi0
+  {
+    double t1 = fnow_ms();
+    const int64_t size = wheel2310().to_index((uint64_t) z) + 1;
+    const int grid = c.num_sms * 8;
+    DevBuf part;
+    part.alloc((size_t) grid * 16);
+    PCG_CUDA(cudaMemsetAsync(part.p, 0, (size_t) grid * 16, s));
+    PhiTab PT = phi_tab(c);
+    if (T.fd_bytes == 2)
+      k_phi0<uint16_t><<<grid, 256, 0, s>>>((uint64_t) x, (uint64_t) (x >> 64), T.factor_d.as<uint16_t>(), size,
+                                            (uint32_t) (2 * k + 1), (uint64_t) T.h_primes[(size_t) k], PT, T.coprime.as<uint16_t>(), part.as<i128>());
+    else
+      k_phi0<uint32_t><<<grid, 256, 0, s>>>((uint64_t) x, (uint64_t) (x >> 64), T.factor_d.as<uint32_t>(), size,
+                                            (uint32_t) (2 * k + 1), (uint64_t) T.h_primes[(size_t) k], PT, T.coprime.as<uint16_t>(), part.as<i128>());
+    PCG_CUDA(cudaGetLastError());
+    R.launches++;
+    R.phi0 = sum_partials(part, grid, s);
+    R.ms_phi0 = fnow_ms() - t1;
+  }
+
+  // ---- Sigma (Sigma.cpp:25-140)
+  {
+    double t1 = fnow_ms();
+    const i128 a = host_pi(T, (uint64_t) y);
+    const i128 b = host_pi(T, (uint64_t) x13);
+    const int64_t sqrt_xy = isqrt(x / (u128) y);
+    std::vector<uint64_t> q;
+    q.push_back((uint64_t) sqrtx);
+    q.push_back((uint64_t) sqrt_xy);
+    // primes in (x_star, x^(1/3)]: arguments of Sigma4..6
+    const int64_t i0 = host_pi(T, (uint64_t) x_star) + 1, i1 = host_pi(T, (uint64_t) x13);
+    for (int64_t i = i0; i <= i1; i++) {
+      const u128 p = T.h_primes[(size_t) i];
+      if ((int64_t) p <= sqrt_xy) q.push_back((uint64_t) (x / (p * (u128) y)));
+      else q.push_back((uint64_t) (x / (p * p)));
+      q.push_back((uint64_t) isqrt(x / p));
+    }
+    std::vector<int64_t> r = pi_lookup(c, q, s);
+    const i128 pi_sqrtx = r[0];
+    const i128 cc = r[1];
+    const i128 d = host_pi(T, (uint64_t) x_star);
+    i128 s0 = a - 1 + (pi_sqrtx * (pi_sqrtx - 1)) / 2 - (a * (a - 1)) / 2;
+    i128 s1 = (a - b) * (a - b - 1) / 2;
+    i128 s2 = a * (b - cc - (cc * (cc - 3)) / 2 + (d * (d - 3)) / 2);
+    i128 s3 = (b * (b - 1) * (2 * b - 1)) / 6 - b - (d * (d - 1) * (2 * d - 1)) / 6 + d;
+    i128 s4 = 0, s5 = 0, s6 = 0;
+    size_t j = 2;
+    for (int64_t i = i0; i <= i1; i++) {
+      const int64_t p = T.h_primes[(size_t) i];
+      if (p <= sqrt_xy) s4 += r[j]; else s5 += r[j];
+      j++;
+      s6 += (i128) r[j] * r[j];
+      j++;
+    }
+    R.sigma = s0 + s1 + s2 + s3 + s4 * a + s5 - s6;
+    R.ms_sigma = fnow_ms() - t1;
+  }
+  R.pi = R.ac - R.b + R.d + R.phi0 + R.sigma;
+  return R;
+}
+
+// x <= 1e10 is counted by the sieve directly
+static const int64_t PI_SIEVE_LIMIT = 10000000000ll;
+
+i128 pi_any(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s, pcg_stats* st)
+{
+  double t0 = fnow_ms();
+  i128 r;
+  pcg_stats z{};
+  if (x < 2) r = 0;
+  else if (x <= (u128) PI_SIEVE_LIMIT) {
+    uint64_t l = 0;
+    r = pi_sieve_count(c, (int64_t) x, s, &l);
+    z.kernel_launches = l;
+  } else {
+    PiParts P = pi_gourdon(c, x, tune, s);
+    r = P.pi;
+    z = P.dstats;
+    z.kernel_launches = P.launches;
+  }
+  z.total_ms = fnow_ms() - t0;
+  if (st) *st = z;
+  return r;
+}
+
+// per-term values of Gourdon's formula (for parity tests against the
+// reference's --AC, --B, --Phi0, --Sigma, --D outputs)
+void pi_gourdon_terms(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s, i128 out[6])
+{
+  PiParts P = pi_gourdon(c, x, tune, s);
+  out[0] = P.ac;
+  out[1] = P.b;
+  out[2] = P.d;
+  out[3] = P.phi0;
+  out[4] = P.sigma;
+  out[5] = P.pi;
+}
+
+
+// ================================================================ phi(x, a)
+// phi(x, a) = # of n <= x not divisible by any of the first a primes
+// (reference semantics and shortcuts: src/phi.cpp:341-430).
+//   a <= 8:               the primorial identity (phi_tiny)
+//   a > pi(sqrt(x)):      pi(x) - a + 1 (1 once a >= pi(x))       (phi_pix)
+//   p_{a+1}^4 > x:        1 + (pi(x) - a) + P2(x, a) + P3(x, a), the
+//                         counts of n <= x with 2 and 3 prime factors > p_a
+//   otherwise:            ordinary leaves n <= y plus the special leaves
+//                         x / (p_b m), m <= y < p_b m, of the Legendre
+//                         recursion, the latter by the sweep (mode phi)
+__global__ void k_phi_one(uint64_t x, PhiTab T, i128* out) { *out = dphi_tiny((u128) x, T); }
+
+// P3 outers: i in (a, pi(x^(1/3))], j in [i, pi(sqrt(x / p_i))]
+__global__ void k_outer_P3(uint64_t x, int64_t a, int64_t i1, const uint32_t* __restrict__ primes,
+                           const uint64_t* __restrict__ pibig, PairOuter* __restrict__ outs)
+{
+  const int64_t t = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t i = a + 1 + t;
+  if (i > i1) return;
+  const uint64_t p = primes[i];
+  const uint64_t xp = x / p;
+  PairOuter O;
+  O.xp_lo = xp;
+  O.xp_hi = 0;
+  O.cap = 0;
+  O.b = (int32_t) i;
+  O.mode = 3;
+  O.i_lo = i - 1;
+  O.i_hi = dpi(pibig, (uint64_t) disqrt((u128) xp));
+  if (O.i_hi < O.i_lo) O.i_hi = O.i_lo;
+  outs[t] = O;
+}
+
+int64_t phi_any(Ctx& c, int64_t x, int64_t a, const Tuning& tune, cudaStream_t s)
+{
+  if (x < 1) return 0;
+  if (a < 1) return x;
+  if (a > x / 2) return 1;
+  if (a <= 8) {
+    ensure_phi_tiny(c, (int) a, s);
+    DevBuf o;
+    o.alloc(16);
+    k_phi_one<<<1, 1, 0, s>>>((uint64_t) x, phi_tab(c), o.as<i128>());
+    PCG_CUDA(cudaGetLastError());
+    i128 r = 0;
+    PCG_CUDA(cudaMemcpyAsync(&r, o.p, 16, cudaMemcpyDeviceToHost, s));
+    PCG_CUDA(cudaStreamSynchronize(s));
+    return (int64_t) r;
+  }
+  const int64_t sq = isqrt((u128) x);
+  const int64_t pi_sq = (int64_t) pi_any(c, (u128) sq, tune, s, nullptr);
+  if (a > pi_sq) {
+    const int64_t pix = (int64_t) pi_any(c, (u128) x, tune, s, nullptr);
+    return a >= pix ? 1 : pix - a + 1;
+  }
+  // a <= pi(sqrt x): p_a and p_{a+1} < 2 sqrt(x) + 2 are in the table
+  ensure_prime_tables(c, std::max<int64_t>(2 * sq + 10, 1000), s);
+  if (a + 1 > c.tab.nprimes) fail(PCG_EINTERNAL, "phi: prime table too small");
+  const int64_t pa = c.tab.h_primes[(size_t) a];
+  const int64_t pa1 = c.tab.h_primes[(size_t) a + 1];
+  if ((u128) pa1 * pa1 * pa1 * pa1 > (u128) x) {
+    // 1 + (pi(x) - a) + P2 + P3
+    const int64_t pix = (int64_t) pi_any(c, (u128) x, tune, s, nullptr);
+    ensure_pibig(c, sq + 240, s);
+    // P2 = sum_{a < i <= pi(sqrt x)} (pi(x / p_i) - i + 1)
+    i128 B = 0;
+    {
+      const int64_t n0 = x / sq, n1 = x / (pa + 1) + 1;
+      PsOut o = run_psieve(c, (u128) x, n0, n1, true, pa, sq, s, nullptr);
+      // pi(n) = pi(lo0 - 1) + (primes >= 7 counted by the segments up to n),
+      // plus 2, 3, 5 when the sieve starts at 0 (lo0 is a multiple of 240)
+      i128 run = 3;
+      if (o.lo0 > 0) run = pi_lookup(c, std::vector<uint64_t>{(uint64_t) (o.lo0 - 1)}, s)[0];
+      for (int64_t i = 0; i < o.nseg; i++) {
+        B += (i128) o.l[(size_t) i] + (i128) o.m[(size_t) i] * run;
+        run += o.c[(size_t) i];
+      }
+    }
+    const i128 n2 = pi_sq;
+    const i128 P2 = B - (n2 * (n2 - 1) - (i128) a * (a - 1)) / 2;
+    // P3 = sum_{a < i <= pi(x^(1/3))} sum_{i <= j <= pi(sqrt(x / p_i))} (pi(x / (p_i p_j)) - j + 1)
+    i128 P3 = 0;
+    const int64_t i1 = host_pi(c.tab, (uint64_t) iroot((u128) x, 3));
+    if (i1 > a) {
+      const int64_t n = i1 - a;
+      DevBuf outs, part;
+      outs.alloc((size_t) n * sizeof(PairOuter));
+      k_outer_P3<<<(unsigned) ((n + 127) / 128), 128, 0, s>>>((uint64_t) x, a, i1, c.tab.primes.as<uint32_t>(),
+                                                              c.tab.pibig.as<uint64_t>(), outs.as<PairOuter>());
+      PCG_CUDA(cudaGetLastError());
+      const int grid = (int) std::min<int64_t>(n, (int64_t) c.num_sms * 8);
+      part.alloc((size_t) grid * 16);
+      PCG_CUDA(cudaMemsetAsync(part.p, 0, (size_t) grid * 16, s));
+      k_pairs<<<grid, 256, 0, s>>>(outs.as<PairOuter>(), n, c.tab.primes.as<uint32_t>(), c.tab.pibig.as<uint64_t>(),
+                                   part.as<i128>());
+      PCG_CUDA(cudaGetLastError());
+      P3 = sum_partials(part, grid, s);
+    }
+    return (int64_t) (1 + (i128) (pix - a) + P2 + P3);
+  }
+  // ordinary + special leaves with m <= y
+  const int64_t cc = 8;
+  int64_t y = std::max<int64_t>(pa, std::min<int64_t>(sq - 1, 8 * iroot((u128) x, 3)));
+  y = std::max<int64_t>(y, pa);
+  ensure_prime_tables(c, y, s);
+  ensure_factor_d(c, pa, y, s);
+  ensure_phi_tiny(c, (int) cc, s);
+  i128 s1 = 0;
+  {
+    const Tables& T = c.tab;
+    const int64_t size = wheel2310().to_index((uint64_t) y) + 1;
+    const int grid = c.num_sms * 8;
+    DevBuf part;
+    part.alloc((size_t) grid * 16);
+    PCG_CUDA(cudaMemsetAsync(part.p, 0, (size_t) grid * 16, s));
+    PhiTab PT = phi_tab(c);
+    if (T.fd_bytes == 2)
+      k_phi0<uint16_t><<<grid, 256, 0, s>>>((uint64_t) x, 0, T.factor_d.as<uint16_t>(), size, (uint32_t) (2 * cc + 1),
+                                            (uint64_t) T.h_primes[(size_t) cc], PT, T.coprime.as<uint16_t>(), part.as<i128>());
+    else
+      k_phi0<uint32_t><<<grid, 256, 0, s>>>((uint64_t) x, 0, T.factor_d.as<uint32_t>(), size, (uint32_t) (2 * cc + 1),
+                                            (uint64_t) T.h_primes[(size_t) cc], PT, T.coprime.as<uint16_t>(), part.as<i128>());
+    PCG_CUDA(cudaGetLastError());
+    s1 = sum_partials(part, grid, s);
+  }
+  SweepProblem p;
+  p.gourdon = 2;
+  p.x = (u128) x;
+  p.y = y;
+  p.z = a;
+  p.k = cc;
+  SweepResult r = run_sweep(c, p, tune, s);
+  return (int64_t) (s1 + r.sum);
+}
+
+}  // namespace pcg

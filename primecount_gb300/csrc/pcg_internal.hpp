@@ -83,6 +83,13 @@ struct Tables {
   int64_t fr_y = -1;
   int fr_bytes = 2;
   DevBuf factor_dr;
+  // PiTable up to sqrt(x) for the A, B, C formulas of pi(x) (no primes array)
+  int64_t pibig_limit = -1;
+  DevBuf pibig;
+  // phi(r, k) for r < p_1 * ... * p_k: coprime bits and per-word prefix counts
+  int phik = -1;
+  uint64_t phi_P = 0, phi_tot = 0;
+  DevBuf phi_bits, phi_pref;
   // wheel tables on device
   DevBuf coprime;            // uint16[480]
   DevBuf cindex;             // int16[2310]
@@ -96,6 +103,11 @@ void ensure_prime_tables(Ctx& c, int64_t limit, cudaStream_t s);
 // FactorTableD for (y, z); FactorTable (DR) for y.
 void ensure_factor_d(Ctx& c, int64_t y, int64_t z, cudaStream_t s);
 void ensure_factor_dr(Ctx& c, int64_t y, cudaStream_t s);
+
+// device exclusive scan (uint32 -> uint64), synchronous on s
+void exclusive_scan_u32(const uint32_t* in, int64_t n, uint64_t* out, cudaStream_t s);
+// PiTable {count, bits} over [0, limit] without the primes array
+void build_pitab_only(DevBuf& out, int64_t limit, cudaStream_t s);
 
 // host PiTable lookup on the host copy
 int64_t host_pi(const Tables& t, uint64_t x);
@@ -144,4 +156,15 @@ Ctx& default_ctx();
 Ctx* ctx_from(const pcg_opts* o);
 cudaStream_t stream_from(Ctx& c, const pcg_opts* o);
 
+// Runs f(ctx, stream) and turns internal failures into a pcg_status plus the
+// message for pcg_last_error (defined in api.cpp).
+pcg_status guarded_call(const pcg_opts* opts, void (*fn)(Ctx&, cudaStream_t, void*), void* arg);
+
 }  // namespace pcg
+
+template <class F>
+inline pcg_status pcg_guarded(const pcg_opts* opts, F&& f)
+{
+  auto tramp = [](pcg::Ctx& c, cudaStream_t s, void* a) { (*(F*) a)(c, s); };
+  return pcg::guarded_call(opts, tramp, (void*) &f);
+}

@@ -1,0 +1,137 @@
+// pi_api.cpp -- extern "C" entry points for pi(x), phi(x, a), the batch
+// forms and the libprimecount C API names (include/pcgpu.h).
+#include <cstdio>
+#include <cstring>
+#include <atomic>
+#include <thread>
+
+#include "pcg_internal.hpp"
+
+namespace pcg {
+i128 pi_any(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s, pcg_stats* st);
+void pi_gourdon_terms(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s, i128 out[6]);
+int64_t phi_any(Ctx& c, int64_t x, int64_t a, const Tuning& tune, cudaStream_t s);
+}  // namespace pcg
+
+using namespace pcg;
+
+namespace {
+
+Tuning tune_of(const pcg_opts* o)
+{
+  Tuning t;
+  if (o) {
+    t.segment_words = o->segment_words;
+    t.ctas_per_sm = o->ctas_per_sm;
+    t.cta_threads = o->cta_threads;
+  }
+  return t;
+}
+
+std::atomic<int> g_threads{0};
+
+}  // namespace
+
+extern "C" {
+
+pcg_status pcg_pi(pcg_i128 xi, const pcg_opts* opts, pcg_i128* out)
+{
+  if (!out) return PCG_EINVAL;
+  return pcg_guarded(opts, [&](Ctx& c, cudaStream_t s) {
+    if (xi.hi < 0) { *out = to_pcg(0); return; }       // pi(x) = 0 for x < 2 (negative x included)
+    pcg_stats st{};
+    i128 r = pi_any(c, make_u128(xi), tune_of(opts), s, &st);
+    c.last = st;
+    if (opts && opts->print) std::printf("pi(x) = %s\nSeconds: %.3f\n", to_string(r).c_str(), st.total_ms / 1000);
+    *out = to_pcg(r);
+  });
+}
+
+pcg_status pcg_pi_terms(pcg_i128 xi, const pcg_opts* opts, pcg_i128* out6)
+{
+  if (!out6) return PCG_EINVAL;
+  return pcg_guarded(opts, [&](Ctx& c, cudaStream_t s) {
+    if (xi.hi < 0) fail(PCG_EINVAL, "x must be >= 0");
+    u128 x = make_u128(xi);
+    if (x <= (u128) 10000000000ull) fail(PCG_EINVAL, "pcg_pi_terms needs x > 1e10 (smaller x is counted by a sieve)");
+    i128 t[6];
+    pi_gourdon_terms(c, x, tune_of(opts), s, t);
+    for (int i = 0; i < 6; i++) out6[i] = to_pcg(t[i]);
+  });
+}
+
+pcg_status pcg_phi(int64_t x, int64_t a, const pcg_opts* opts, int64_t* out)
+{
+  if (!out) return PCG_EINVAL;
+  return pcg_guarded(opts, [&](Ctx& c, cudaStream_t s) { *out = phi_any(c, x, a, tune_of(opts), s); });
+}
+
+pcg_status pcg_pi_batch(const pcg_i128* xs, size_t n, pcg_i128* out, const pcg_opts* opts)
+{
+  if ((!xs || !out) && n) return PCG_EINVAL;
+  for (size_t i = 0; i < n; i++) {
+    pcg_status st = pcg_pi(xs[i], opts, &out[i]);
+    if (st != PCG_OK) return st;
+  }
+  return PCG_OK;
+}
+
+pcg_status pcg_phi_batch(const int64_t* x, const int64_t* a, size_t n, int64_t* out, const pcg_opts* opts)
+{
+  if ((!x || !a || !out) && n) return PCG_EINVAL;
+  for (size_t i = 0; i < n; i++) {
+    pcg_status st = pcg_phi(x[i], a[i], opts, &out[i]);
+    if (st != PCG_OK) return st;
+  }
+  return PCG_OK;
+}
+
+// ---- libprimecount C API: same names; errors print to stderr and return -1
+// (src/api_c.cpp:19-150)
+int64_t primecount_pi(int64_t x)
+{
+  pcg_i128 r;
+  pcg_i128 xi;
+  xi.lo = (uint64_t) x;
+  xi.hi = x < 0 ? -1 : 0;
+  if (pcg_pi(xi, nullptr, &r) != PCG_OK) {
+    std::fprintf(stderr, "primecount_pi: %s\n", pcg_last_error(nullptr));
+    return -1;
+  }
+  return (int64_t) r.lo;
+}
+
+pcg_i128 primecount_pi_128(pcg_i128 x)
+{
+  pcg_i128 r;
+  if (pcg_pi(x, nullptr, &r) != PCG_OK) {
+    std::fprintf(stderr, "primecount_pi_128: %s\n", pcg_last_error(nullptr));
+    r.lo = ~0ull;
+    r.hi = -1;
+  }
+  return r;
+}
+
+int64_t primecount_phi(int64_t x, int64_t a)
+{
+  int64_t r = 0;
+  if (pcg_phi(x, a, nullptr, &r) != PCG_OK) {
+    std::fprintf(stderr, "primecount_phi: %s\n", pcg_last_error(nullptr));
+    return -1;
+  }
+  return r;
+}
+
+int primecount_get_num_threads(void)
+{
+  int t = g_threads.load();
+  if (t > 0) return t;
+  unsigned h = std::thread::hardware_concurrency();
+  return h ? (int) h : 1;
+}
+
+void primecount_set_num_threads(int num_threads) { g_threads.store(num_threads > 0 ? num_threads : 0); }
+
+const char* primecount_version(void) { return "8.7"; }
+
+}  // extern "C"

@@ -35,75 +35,9 @@
 #include <string>
 
 #include "pcg_internal.hpp"
+#include "dev_common.cuh"
 
 namespace pcg {
-
-// ---------------------------------------------------------------- constants
-// # of wheel offsets {1,7,11,13,17,19,23,29} that are <= t, for t in [0, 30):
-// nibble t of these two words.
-#define PCG_CNT8_LO 0x4443322221111110ull
-#define PCG_CNT8_HI 0x0087777776666554ull
-// wheel offsets packed as bytes
-#define PCG_WOFF 0x1D1713110D0B0701ull
-
-__device__ __forceinline__ uint32_t cnt8(uint32_t t)
-{
-  uint64_t v = t < 16 ? PCG_CNT8_LO : PCG_CNT8_HI;
-  uint32_t sh = (t < 16 ? t : t - 16) * 4;
-  return (uint32_t) (v >> sh) & 15u;
-}
-
-// bits of a 240-block for the numbers <= r (r in [0, 240))
-__device__ __forceinline__ uint64_t mask_le(uint32_t r)
-{
-  uint32_t byte = r / 30;
-  uint32_t nb = byte * 8 + cnt8(r - byte * 30);
-  return nb >= 64 ? ~0ull : ((1ull << nb) - 1);
-}
-
-__device__ __forceinline__ uint32_t woff(uint32_t j) { return (uint32_t) (PCG_WOFF >> (8 * j)) & 0xFFu; }
-
-// # numbers in [1, q] coprime to 30
-__device__ __forceinline__ uint64_t cnt_le(uint64_t q) { return 8 * (q / 30) + cnt8((uint32_t) (q % 30)); }
-
-// bit of number offset `off` (coprime to 30) inside its word
-__device__ __forceinline__ uint32_t bit_of(uint32_t r) { return (r / 30) * 8 + cnt8(r % 30) - 1; }
-
-// PiTable lookup: {count, bits} per 240 numbers (count includes 2, 3, 5)
-__device__ __forceinline__ int64_t dpi(const uint64_t* __restrict__ pt, uint64_t x)
-{
-  if (x < 6) return (0x322100u >> (4 * x)) & 15u;
-  uint64_t i = x / 240;
-  return (int64_t) (pt[2 * i] + __popcll(pt[2 * i + 1] & mask_le((uint32_t) (x - 240 * i))));
-}
-
-__device__ __forceinline__ int64_t dmin(int64_t a, int64_t b) { return a < b ? a : b; }
-__device__ __forceinline__ int64_t dmax(int64_t a, int64_t b) { return a > b ? a : b; }
-
-// exact floor(sqrt(x)) for x < 2^126
-__device__ int64_t disqrt(u128 x)
-{
-  if (x == 0) return 0;
-  int64_t r = (int64_t) sqrt((double) x);
-  while (r > 0 && (u128) r * (u128) r > x) r--;
-  while ((u128) (r + 1) * (u128) (r + 1) <= x) r++;
-  return r;
-}
-
-// min(floor(a / d), cap) for d >= 1, cap >= 0
-__device__ __forceinline__ int64_t divcap(u128 a, uint64_t d, int64_t cap)
-{
-  if ((u128) d * (u128) cap <= a) return cap;
-  if ((uint64_t) (a >> 64) == 0) return (int64_t) ((uint64_t) a / d);
-  return (int64_t) (a / d);
-}
-
-// a / d for a 128-bit a, 64-bit division when the high word is zero
-__device__ __forceinline__ u128 div128(u128 a, uint64_t d)
-{
-  if ((uint64_t) (a >> 64) == 0) return (u128) ((uint64_t) a / d);
-  return a / d;
-}
 
 // ================================================================ prime tables
 // PiTable bits: word w holds the primes >= 7 among 240w + {1,7,...}
@@ -559,7 +493,12 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 2 : ((NT >= 256) ? 3 : 4)) k
 
     // level bounds of this segment (chunk bounds of D.cpp:83-94 / S2_hard.cpp:64-71)
     int64_t bmin_leaf, bmax_leaf, bcnt;
-    if (A.gourdon) {
+    if (A.gourdon == 2) {
+      // phi(x, a) special leaves: p_b <= p_a (held in x_star), m <= y
+      bmax_leaf = dpi(A.pitab, (uint64_t) dmin(disqrt(div128(x, (uint64_t) low1)), A.x_star));
+      bmin_leaf = dpi(A.pitab, (uint64_t) dmin(A.L / high, A.x_star));
+      bcnt = dpi(A.pitab, (uint64_t) dmin(disqrt(div128(x, (uint64_t) high)), A.x_star));
+    } else if (A.gourdon) {
       bmax_leaf = dpi(A.pitab, (uint64_t) dmin(dmin(disqrt(div128(x, (uint64_t) low1)), disqrt((u128) high)), A.x_star));
       bmin_leaf = dpi(A.pitab, (uint64_t) dmin(A.L / high, A.x_star));
       bcnt = dpi(A.pitab, (uint64_t) dmin(disqrt(div128(x, (uint64_t) high)), A.x_star));
@@ -641,7 +580,13 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 2 : ((NT >= 256) ? 3 : 4)) k
             bool stop = false;
             if (b <= A.pi_sqrt) {
               int64_t min_m, max_m;
-              if (A.gourdon) {
+              if (A.gourdon == 2) {
+                // phi(x, a): m in (max(y / p, x / (p high)), min(y, x / (p low))]
+                int64_t xp_high = divcap(xp, (uint64_t) high, A.y);
+                min_m = dmax(xp_high, A.y / prime);
+                max_m = divcap(xp, (uint64_t) low1, A.y);
+                P.thr = (uint32_t) (2 * b + 1);
+              } else if (A.gourdon) {
                 int64_t xp_low = divcap(xp, (uint64_t) low1, A.z);
                 int64_t xp_high = divcap(xp, (uint64_t) high, A.z);
                 min_m = dmax(xp_high, A.z / prime);
@@ -1064,6 +1009,55 @@ void ensure_prime_tables(Ctx& c, int64_t limit, cudaStream_t s)
   t.build_ms += now_ms() - t0;
 }
 
+void exclusive_scan_u32(const uint32_t* in, int64_t n, uint64_t* out, cudaStream_t s)
+{
+  int64_t nblk = (n + SCAN_ITEMS - 1) / SCAN_ITEMS;
+  DevBuf sums;
+  sums.alloc((size_t) std::max<int64_t>(nblk, 1) * 8);
+  k_scan_sums<<<(unsigned) nblk, 512, 0, s>>>(in, n, sums.as<uint64_t>());
+  k_scan_serial<<<1, 1024, 0, s>>>(sums.as<uint64_t>(), nblk);
+  k_scan_apply<<<(unsigned) nblk, 512, 0, s>>>(in, n, sums.as<uint64_t>(), out);
+  PCG_CUDA(cudaGetLastError());
+  PCG_CUDA(cudaStreamSynchronize(s));
+}
+
+__global__ void k_pitab_pack(const uint64_t* __restrict__ bits, const uint64_t* __restrict__ excl, int64_t nwords,
+                             uint64_t* __restrict__ pitab)
+{
+  int64_t w = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nwords) return;
+  pitab[2 * w] = 3 + excl[w];
+  pitab[2 * w + 1] = bits[w];
+}
+
+// PiTable {count, bits} per 240 numbers over [0, limit] without the primes
+// array (for the lookups of pi(n), n <= sqrt(x), of the A, B, C formulas).
+void build_pitab_only(DevBuf& out, int64_t limit, cudaStream_t s)
+{
+  limit = std::max<int64_t>(limit, 240 * 4);
+  int64_t nwords = limit / 240 + 1;
+  std::vector<uint32_t> base = small_primes(isqrt((u128) limit) + 1);
+  std::vector<uint32_t> b7;
+  for (uint32_t p : base) if (p >= 7) b7.push_back(p);
+  DevBuf d_base, d_bits, d_pc, d_excl;
+  d_base.alloc(std::max<size_t>(b7.size(), 1) * 4);
+  d_bits.alloc((size_t) nwords * 8);
+  d_pc.alloc((size_t) nwords * 4);
+  d_excl.alloc((size_t) nwords * 8);
+  if (!b7.empty())
+    PCG_CUDA(cudaMemcpyAsync(d_base.p, b7.data(), b7.size() * 4, cudaMemcpyHostToDevice, s));
+  int64_t pblocks = (nwords + 2047) / 2048;
+  k_prime_bits<<<(unsigned) pblocks, 512, 2048 * 8, s>>>(d_bits.as<uint64_t>(), d_pc.as<uint32_t>(), nwords, limit,
+                                                         d_base.as<uint32_t>(), (int) b7.size());
+  PCG_CUDA(cudaGetLastError());
+  exclusive_scan_u32(d_pc.as<uint32_t>(), nwords, d_excl.as<uint64_t>(), s);
+  out.alloc((size_t) nwords * 16);
+  k_pitab_pack<<<(unsigned) ((nwords + 255) / 256), 256, 0, s>>>(d_bits.as<uint64_t>(), d_excl.as<uint64_t>(), nwords,
+                                                                 out.as<uint64_t>());
+  PCG_CUDA(cudaGetLastError());
+  PCG_CUDA(cudaStreamSynchronize(s));
+}
+
 template <typename T>
 static void build_factor(Ctx& c, DevBuf& out, int64_t limit, int64_t y, int gourdon, cudaStream_t s)
 {
@@ -1175,7 +1169,8 @@ static std::vector<int64_t> plan_segments(const SweepProblem& pb, const Tables& 
     for (int64_t b = pb.k + 1; b <= bglob; b++) {
       const double p = pr[b], xp = x / p;
       double mlo, mhi;
-      if (pb.gourdon) {
+      if (pb.gourdon == 2) { mlo = std::max(y / p, xp / hi); mhi = std::min(xp / l1, y); }
+      else if (pb.gourdon) {
         if (b <= pi_sqrt) { mlo = std::max(z / p, xp / hi); mhi = std::min({xp / (p * p), z, xp / l1}); }
         else { mlo = std::max(p, xp / hi); mhi = std::min({xp / (p * p), y, xp / l1}); }
       } else {
@@ -1190,6 +1185,7 @@ static std::vector<int64_t> plan_segments(const SweepProblem& pb, const Tables& 
   auto levels = [&](double a) {
     double lim = pb.gourdon ? std::min((double) x_star, std::sqrt(x / std::max(a, 1.0)))
                             : std::min(std::sqrt(z), std::sqrt(x / std::max(a, 1.0)));
+    if (pb.gourdon == 2) lim = std::min((double) x_star, std::sqrt(x / std::max(a, 1.0)));
     return (double) host_pi(t, (uint64_t) std::min(lim, (double) t.prime_limit));
   };
   const double c_level = 30.0;
@@ -1242,7 +1238,17 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   const u128 x = pb.x;
   int64_t L, x_star = 0, pi_sqrt, bglob;
   int64_t pi_limit;
-  if (pb.gourdon) {
+  if (pb.gourdon == 2) {
+    // phi(x, a) special leaves: y = pb.y (m <= y), a = pb.z, c = pb.k;
+    // FactorTableD built with the prime-factor limit p_a over n <= y
+    L = (int64_t) (x / (u128) pb.y);
+    pi_limit = pb.y;
+    ensure_prime_tables(c, pi_limit, s);
+    x_star = c.tab.h_primes[(size_t) pb.z];   // p_a
+    ensure_factor_d(c, x_star, pb.y, s);
+    pi_sqrt = pb.z;
+    bglob = pb.z;
+  } else if (pb.gourdon) {
     L = (int64_t) (x / (u128) pb.z);
     x_star = x_star_gourdon(x, pb.y);
     pi_limit = pb.y;

@@ -63,7 +63,7 @@ def run_status(x, opt):
     lines = [l for l in out.splitlines() if l.strip()]
     res = int(lines[-1]) if re.fullmatch(r"-?\d+", lines[-1].strip()) else None
     if res is None:
-        m = re.findall(r"^(?:D|S2_hard) = (-?\d+)$", out, re.M)
+        m = re.findall(r"^(?:D|S2_hard|A \+ C|B|Phi0|Sigma) = (-?\d+)$", out, re.M)
         res = int(m[-1])
     return res, vars_
 
@@ -151,6 +151,24 @@ def main():
             a_ = rng.randint(1, max(1, pis_q))
             rows.append([x, a_, int(run(["--phi", x, a_]).strip().splitlines()[-1])])
         data["phi_random"] = rows
+
+    # Gourdon's other terms, to pin pi(x) term by term (--AC, --B, --Phi0,
+    # --Sigma print the reference's own value of each formula)
+    if "gourdon_parts" not in data:
+        rng = random.Random(20261207)
+        xs = [10 ** e for e in range(8, 19)] + [int(10 ** rng.uniform(8, 17)) for _ in range(24)]
+        rows = []
+        for x in xs:
+            row = {"x": x}
+            for opt, key in (("--AC", "AC"), ("--B", "B"), ("--Phi0", "Phi0"), ("--Sigma", "Sigma")):
+                r, v = run_status(x, opt)
+                row[key] = r
+                row.update({"y": int(v["y"]), "z": int(v["z"]), "k": int(v["k"])} if "z" in v else {"y": int(v["y"])})
+            row["D"] = run_status(x, "--D")[0]
+            row["pi"] = int(run([x]).strip().splitlines()[-1])
+            rows.append(row)
+            print("parts", row, flush=True)
+        data["gourdon_parts"] = rows
 
     json.dump(data, open(OUT, "w"), indent=1)
     print("wrote", OUT)

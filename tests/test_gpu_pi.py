@@ -1,0 +1,74 @@
+"""GPU parity: pi(x) and phi(x, a) through the C ABI against the reference's
+published values, fixtures made by the reference binary, and the oracle."""
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_pi_powers_of_ten(pcg, golden):
+    # README.md:163-277 of the reference: pi(10^n)
+    for xs, v in golden["pi_pow10"].items():
+        x = int(xs)
+        if x <= 10 ** 19:
+            assert pcg.pi(x) == v, xs
+
+
+def test_pi_random_fixture(pcg, golden):
+    for x, v in golden["pi_random"]:
+        assert pcg.pi(x) == v, x
+
+
+def test_gourdon_terms_match_reference(pcg, golden):
+    # each term against the reference's --AC, --B, --D, --Phi0, --Sigma
+    rows = golden.get("gourdon_parts", [])
+    if not rows:
+        pytest.skip("fixture has no gourdon_parts yet")
+    for row in rows:
+        x = row["x"]
+        if x <= 10 ** 10:
+            continue
+        t = pcg.pi_terms(x)
+        for k in ("AC", "B", "D", "Phi0", "Sigma", "pi"):
+            assert t[k] == row[k], (x, k, t[k], row[k])
+
+
+def test_pi_small_x_against_oracle(pcg, ora):
+    xs = list(range(-5, 2000, 3)) + [30719, 65536, 10 ** 6 + 3]
+    got = pcg.pi_batch(xs)
+    for x, v in zip(xs, got):
+        assert v == (ora.pi_sieve(x) if x >= 2 else 0), x
+
+
+def test_pi_c_api(pcg):
+    L = pcg.load()
+    assert L.primecount_pi(10 ** 12) == 37607912018
+    r = L.primecount_pi_128(pcg.to_i128(10 ** 11))
+    assert pcg.from_i128(r) == 4118054813
+    assert L.primecount_version() == b"8.7"
+
+
+def test_phi_api_golden(pcg, golden):
+    for x, a, v in golden["phi_api"]:
+        assert pcg.phi(x, a) == v
+
+
+def test_phi_random_fixture(pcg, golden):
+    for x, a, v in golden["phi_random"]:
+        assert pcg.phi(x, a) == v, (x, a)
+
+
+def test_phi_edge_cases(pcg, ora):
+    for x, a in [(0, 5), (-3, 2), (100, 0), (100, -1), (100, 60), (1000, 1), (1000, 8), (10 ** 6, 3),
+                 (10 ** 6, 168), (10 ** 6, 169), (10 ** 6, 78498), (10 ** 6, 78499), (10 ** 7, 30), (10 ** 7, 447)]:
+        want = ora.phi(x, a) if x >= 1 else 0
+        assert pcg.phi(x, a) == want, (x, a)
+
+
+def test_phi_all_regimes_against_oracle(pcg, ora):
+    # a <= 8, small a (special leaves), p_a >= x^(1/4) (P2 + P3), a > pi(sqrt x)
+    import random
+    rng = random.Random(11)
+    for _ in range(30):
+        x = int(10 ** rng.uniform(6, 9))
+        a = rng.choice([rng.randint(1, 8), rng.randint(9, 40), rng.randint(40, 1200)])
+        assert pcg.phi(x, a) == ora.phi(x, a), (x, a)
