@@ -34,7 +34,7 @@ sys.path.insert(0, ROOT)
 
 X = 10 ** 20
 WORKLOAD = "D(1e20) hard special leaves, Gourdon default parameters (y=z=245535363, k=8)"
-METRIC = "D(1e20) hard-leaves/s on 1 GB300"
+METRIC = "pi(1e20) sec & hard-leaves/s on 1 GB300"
 UNIT = "hard-leaves/s"
 TOTAL_LEAVES_1E20 = 22178370075
 
@@ -101,10 +101,11 @@ def cpu_baseline(p, threads, target_s=12.0):
     import oracle
     oracle.load()
     nchunks = max(64, 4 * threads)
-    frac = 2e-4
+    frac = 1e-4
     leaves, secs = oracle.D_sample(X, p["y"], p["z"], p["k"], nchunks, frac, threads)
-    if secs > 0 and secs < target_s / 4:
-        frac = min(0.05, frac * target_s / max(secs, 1e-3))
+    # grow the sample until it takes about target_s (at most 10x per step)
+    while secs < target_s / 3 and frac < 0.05:
+        frac = min(0.05, frac * min(10.0, 0.8 * target_s / max(secs, 1e-3)))
         leaves, secs = oracle.D_sample(X, p["y"], p["z"], p["k"], nchunks, frac, threads)
     est_total_s = secs / frac
     return {"value": TOTAL_LEAVES_1E20 / est_total_s, "unit": UNIT, "cores": threads, "kind": "port",
@@ -147,6 +148,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--x", default="1e20", help="smaller x for profiling runs (the headline is 1e20)")
+    ap.add_argument("--pi-steps", type=int, default=1, help="pi(x) end-to-end repetitions")
     args = ap.parse_args()
     global X
     X = int(float(args.x)) if "e" in args.x else int(args.x)
@@ -236,6 +238,23 @@ def main():
         assert v2 == v
     e2e_s = sum(e2e_t) / len(e2e_t) if e2e_t else float("nan")
 
+    # pi(x) end to end through the C ABI (pcg_pi, fresh context: every table
+    # built inside the call), with the time of each Gourdon term
+    pi_line = None
+    if args.pi_steps > 0:
+        ts = []
+        for _ in range(args.pi_steps):
+            c3 = pcg.Context(0)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            pv = pcg.pi(X, ctx=c3)
+            ts.append(time.perf_counter() - t1)
+            s3 = c3.last_stats()
+            c3.close()
+        pi_line = {"x": args.x, "pi": str(pv), "seconds": min(ts), "seconds_all": ts,
+                   "terms_ms": {"D": s3["d_ms"], "AC": s3["ac_ms"], "B": s3["b_ms"], "Phi0": s3["phi0_ms"],
+                                "Sigma": s3["sigma_ms"], "tables": s3["table_ms"]}}
+
     if rank != 0:
         return
     peak, peak_kind = measured_peaks()
@@ -261,6 +280,7 @@ def main():
             "result": str(v), "leaves_per_step": leaves,
             "e2e": {"value": leaves / e2e_s, "unit": UNIT, "seconds": e2e_s,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "pi_e2e": pi_line,
             "gpu_launches": int(st["kernel_launches"]) * args.steps,
             "roofline": roof, "cpu_baseline": cpu,
             "clocks": summarize_clocks(rows, torch.cuda.current_device()),

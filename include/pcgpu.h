@@ -89,6 +89,7 @@ typedef struct {
   int segment_words;       /* tuning actually used                                    */
   int ctas_per_sm;
   int threads_per_cta;
+  double ac_ms, b_ms, phi0_ms, sigma_ms, d_ms; /* pi(x): time of each Gourdon term   */
 } pcg_stats;
 
 /* ---- contexts: device-resident prime / PiTable / FactorTable state ---- */

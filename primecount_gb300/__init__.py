@@ -52,7 +52,8 @@ class Stats(ctypes.Structure):
                 ("sweep_kernel_ms", ctypes.c_double), ("sweep_launches", ctypes.c_uint64),
                 ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
                 ("segment_words", ctypes.c_int), ("ctas_per_sm", ctypes.c_int),
-                ("threads_per_cta", ctypes.c_int)]
+                ("threads_per_cta", ctypes.c_int), ("ac_ms", ctypes.c_double), ("b_ms", ctypes.c_double),
+                ("phi0_ms", ctypes.c_double), ("sigma_ms", ctypes.c_double), ("d_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -831,6 +831,12 @@ i128 pi_any(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s, pcg_stats* st)
     r = P.pi;
     z = P.dstats;
     z.kernel_launches = P.launches;
+    z.table_ms = P.ms_tables;
+    z.ac_ms = P.ms_ac;
+    z.b_ms = P.ms_b;
+    z.phi0_ms = P.ms_phi0;
+    z.sigma_ms = P.ms_sigma;
+    z.d_ms = P.ms_d;
   }
   z.total_ms = fnow_ms() - t0;
   if (st) *st = z;

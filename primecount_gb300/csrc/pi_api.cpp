@@ -2,8 +2,11 @@
 // forms and the libprimecount C API names (include/pcgpu.h).
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <atomic>
+#include <mutex>
 #include <thread>
+#include <vector>
 
 #include "pcg_internal.hpp"
 
@@ -66,25 +69,112 @@ pcg_status pcg_phi(int64_t x, int64_t a, const pcg_opts* opts, int64_t* out)
   return pcg_guarded(opts, [&](Ctx& c, cudaStream_t s) { *out = phi_any(c, x, a, tune_of(opts), s); });
 }
 
+}  // extern "C"
+
+// Batches: the queries run largest first on a pool of worker contexts, each
+// with its own stream and its own device-resident tables sized for the
+// largest x of the batch, so that the short launch sequences of small queries
+// overlap on the GPU.  Results do not depend on the pool: each query is
+// computed exactly as alone.
+namespace {
+
+struct WorkerPool {
+  std::mutex mu;
+  std::vector<pcg::Ctx*> ctx;
+  int device = -1;
+};
+WorkerPool g_pool;
+
+int pool_size(const pcg_opts* opts, size_t n)
+{
+  int w = (opts && opts->threads > 0) ? opts->threads : 4;
+  w = std::max(1, std::min(w, 16));
+  return (int) std::min<size_t>((size_t) w, std::max<size_t>(n, 1));
+}
+
+template <class F>
+pcg_status run_pool(size_t n, const pcg_opts* opts, const std::vector<size_t>& order, F&& job)
+{
+  const int W = pool_size(opts, n);
+  std::lock_guard<std::mutex> g(g_pool.mu);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return PCG_ENODEV; }
+  if (g_pool.device != dev) {
+    for (auto* c : g_pool.ctx) pcg_ctx_destroy((pcg_ctx*) c);
+    g_pool.ctx.clear();
+    g_pool.device = dev;
+  }
+  while ((int) g_pool.ctx.size() < W) {
+    pcg_ctx* c = nullptr;
+    pcg_i128 zero;
+    zero.lo = 0;
+    zero.hi = 0;
+    pcg_status st = pcg_ctx_create(zero, 0, &c);
+    if (st != PCG_OK) return st;
+    g_pool.ctx.push_back((pcg::Ctx*) c);
+  }
+  std::atomic<size_t> next{0};
+  std::atomic<int> err{PCG_OK};
+  std::string msg;
+  std::mutex msg_mu;
+  std::vector<std::thread> th;
+  for (int w = 0; w < W; w++) {
+    th.emplace_back([&, w] {
+      pcg_opts o{};
+      if (opts) o = *opts;
+      o.ctx = (pcg_ctx*) g_pool.ctx[(size_t) w];
+      o.stream = nullptr;
+      for (;;) {
+        const size_t k = next.fetch_add(1);
+        if (k >= n || err.load() != PCG_OK) break;
+        pcg_status st = job(order[k], &o);
+        if (st != PCG_OK) {
+          int expected = PCG_OK;
+          if (err.compare_exchange_strong(expected, (int) st)) {
+            std::lock_guard<std::mutex> lk(msg_mu);
+            msg = pcg_last_error(o.ctx);
+          }
+          break;
+        }
+      }
+    });
+  }
+  for (auto& t : th) t.join();
+  if (err.load() != PCG_OK) return (pcg_status) err.load();
+  return PCG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 pcg_status pcg_pi_batch(const pcg_i128* xs, size_t n, pcg_i128* out, const pcg_opts* opts)
 {
   if ((!xs || !out) && n) return PCG_EINVAL;
-  for (size_t i = 0; i < n; i++) {
-    pcg_status st = pcg_pi(xs[i], opts, &out[i]);
-    if (st != PCG_OK) return st;
-  }
-  return PCG_OK;
+  if (n == 0) return PCG_OK;
+  std::vector<size_t> order(n);
+  for (size_t i = 0; i < n; i++) order[i] = i;
+  auto key = [&](size_t i) { return make_u128(xs[i]); };
+  std::sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+    if (xs[a].hi < 0 || xs[b].hi < 0) return xs[a].hi > xs[b].hi;
+    return key(a) > key(b);
+  });
+  return run_pool(n, opts, order, [&](size_t i, const pcg_opts* o) { return pcg_pi(xs[i], o, &out[i]); });
 }
 
 pcg_status pcg_phi_batch(const int64_t* x, const int64_t* a, size_t n, int64_t* out, const pcg_opts* opts)
 {
   if ((!x || !a || !out) && n) return PCG_EINVAL;
-  for (size_t i = 0; i < n; i++) {
-    pcg_status st = pcg_phi(x[i], a[i], opts, &out[i]);
-    if (st != PCG_OK) return st;
-  }
-  return PCG_OK;
+  if (n == 0) return PCG_OK;
+  std::vector<size_t> order(n);
+  for (size_t i = 0; i < n; i++) order[i] = i;
+  std::sort(order.begin(), order.end(), [&](size_t p, size_t q) { return x[p] > x[q]; });
+  return run_pool(n, opts, order, [&](size_t i, const pcg_opts* o) { return pcg_phi(x[i], a[i], o, &out[i]); });
 }
+
+}  // extern "C"
+
+extern "C" {
 
 // ---- libprimecount C API: same names; errors print to stderr and return -1
 // (src/api_c.cpp:19-150)
