@@ -115,6 +115,61 @@ def cpu_baseline(p, threads, target_s=12.0):
             "sample_seconds": secs, "est_total_seconds": est_total_s}
 
 
+def batch_workload(n, seed=20261203):
+    """Seeded batch: n pi(x), x = 10^U(10,18); n phi(x, a), x = 10^U(8,16),
+    a = U{1, pi(sqrt x)} (std::mt19937_64 is not needed for determinism:
+    Python's seeded generator fixes the inputs and they are printed in the
+    config)."""
+    import math
+    import random
+    rng = random.Random(seed)
+    xs = [int(10 ** rng.uniform(10, 18)) for _ in range(n)]
+    px = [int(10 ** rng.uniform(8, 16)) for _ in range(n)]
+    us = [rng.random() for _ in range(n)]
+    return xs, px, us
+
+
+def run_batch(args, pcg):
+    import math
+    import torch
+    n = args.batch
+    xs, px, us = batch_workload(n)
+    sq = [math.isqrt(x) for x in px]
+    pis = pcg.pi_batch(sq)
+    pa = [1 + int(u * max(1, p)) for u, p in zip(us, pis)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r_pi = pcg.pi_batch(xs)
+    t1 = time.perf_counter()
+    r_phi = pcg.phi_batch(px, pa)
+    t2 = time.perf_counter()
+    m = min(args.plain_sample, n)
+    # plain: one query per call, tables built inside (fresh context)
+    tp = []
+    for i in range(m):
+        c = pcg.Context(0)
+        a0 = time.perf_counter()
+        v = pcg.pi(xs[i], ctx=c)
+        tp.append(("pi", time.perf_counter() - a0))
+        assert v == r_pi[i]
+        c.close()
+        c = pcg.Context(0)
+        a0 = time.perf_counter()
+        v = pcg.phi(px[i], pa[i], ctx=c)
+        tp.append(("phi", time.perf_counter() - a0))
+        assert v == r_phi[i]
+        c.close()
+    plain_pi = [t for k, t in tp if k == "pi"]
+    plain_phi = [t for k, t in tp if k == "phi"]
+    return {"queries": {"pi": n, "phi": n}, "seed": 20261203,
+            "engine": {"pi_qps": n / (t1 - t0), "phi_qps": n / (t2 - t1), "all_qps": 2 * n / (t2 - t0),
+                       "seconds": t2 - t0},
+            "plain_sample": {"queries_per_kind": m, "pi_qps": len(plain_pi) / max(sum(plain_pi), 1e-9),
+                             "phi_qps": len(plain_phi) / max(sum(plain_phi), 1e-9),
+                             "note": "first queries of the same seeded batch, one per call, fresh context"},
+            "checks": "plain answers equal the batched ones on the sample"}
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -149,6 +204,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--x", default="1e20", help="smaller x for profiling runs (the headline is 1e20)")
     ap.add_argument("--pi-steps", type=int, default=1, help="pi(x) end-to-end repetitions")
+    ap.add_argument("--batch", type=int, default=256,
+                    help="queries per kind of the batched workload (4096 = the full config; 0 = skip)")
+    ap.add_argument("--plain-sample", type=int, default=24, help="queries per kind timed in the plain form")
+    ap.add_argument("--serve-seconds", type=float, default=0, help="serving stream length (0 = skip)")
     args = ap.parse_args()
     global X
     X = int(float(args.x)) if "e" in args.x else int(args.x)
@@ -255,6 +314,16 @@ def main():
                    "terms_ms": {"D": s3["d_ms"], "AC": s3["ac_ms"], "B": s3["b_ms"], "Phi0": s3["phi0_ms"],
                                 "Sigma": s3["sigma_ms"], "tables": s3["table_ms"]}}
 
+    batch = run_batch(args, pcg) if args.batch > 0 else None
+    serve = None
+    if args.serve_seconds > 0:
+        from primecount_gb300 import serve as sv
+        stream = sv.make_stream(20261203, 2000, args.serve_seconds)
+        r = sv.run_served(stream, workers=4, max_x=10 ** 20, drain_s=30)
+        r.pop("results")
+        serve = {"served": r, "config": {"rate": 2000, "seconds": args.serve_seconds, "seed": 20261203,
+                                         "pi_x": "10^U(8,20)", "phi_x": "10^U(8,16)", "requests": len(stream)}}
+
     if rank != 0:
         return
     peak, peak_kind = measured_peaks()
@@ -281,6 +350,8 @@ def main():
             "e2e": {"value": leaves / e2e_s, "unit": UNIT, "seconds": e2e_s,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "pi_e2e": pi_line,
+            "batch": batch,
+            "serve": serve,
             "gpu_launches": int(st["kernel_launches"]) * args.steps,
             "roofline": roof, "cpu_baseline": cpu,
             "clocks": summarize_clocks(rows, torch.cuda.current_device()),
