@@ -103,9 +103,12 @@ def cpu_baseline(p, threads, target_s=12.0):
     nchunks = max(64, 4 * threads)
     frac = 1e-4
     leaves, secs = oracle.D_sample(X, p["y"], p["z"], p["k"], nchunks, frac, threads)
-    # grow the sample until it takes about target_s (at most 10x per step)
+    # grow the sample until it takes about target_s: at most 10x per step while
+    # the sample is tiny, 3x once it takes 0.3 s (its cost grows faster than
+    # linearly with the fraction)
     while secs < target_s / 3 and frac < 0.05:
-        frac = min(0.05, frac * min(10.0, 0.8 * target_s / max(secs, 1e-3)))
+        step = min(10.0 if secs < 0.3 else 3.0, 0.8 * target_s / max(secs, 1e-3))
+        frac = min(0.05, frac * step)
         leaves, secs = oracle.D_sample(X, p["y"], p["z"], p["k"], nchunks, frac, threads)
     est_total_s = secs / frac
     return {"value": TOTAL_LEAVES_1E20 / est_total_s, "unit": UNIT, "cores": threads, "kind": "port",

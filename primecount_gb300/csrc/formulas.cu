@@ -345,23 +345,38 @@ __global__ void k_outer_C2(AcParams P, PairOuter* __restrict__ outs)
 
 // ---------------------------------------------------------------- prime sieve segments (B, small pi)
 // Each CTA sieves a segment [lo, hi) (lo a multiple of 240) of the numbers
-// coprime to 30 with every prime 7 <= p <= sqrt(hi), leaving the primes.
-// Mode count: seg_c[s] = # primes >= 7 in the segment.  Mode B additionally
-// answers the queries x / p for the primes p in (max(y, x / hi), min(sqrt(x),
-// x / lo)] (enumerated from the PiTable bits up to sqrt(x)): seg_m[s] = # of
-// them, seg_l[s] = sum of # primes in [lo, x / p].
-#define PS_WORDS 16384
+// coprime to 30, leaving the primes.  Mode count: seg_c[s] = # primes >= 7 in
+// the segment.  Mode B additionally answers the queries x / p for the primes p
+// in (max(qlo, x / hi), min(qhi, x / lo)] (enumerated from the PiTable bits up
+// to sqrt(x)): seg_m[s] = # of them, seg_l[s] = sum of # primes in [lo, x / p].
+//
+// Cross-off in three tiers:
+//  * 7..61: each word starts as the AND of the primes' wheel patterns (the
+//    multiples of p repeat every p words of 240 numbers);
+//  * 67 <= p < mid_limit: a warp per prime, lane l owning the multiples p q
+//    with q = c_l (mod 120), c_l the l-th residue coprime to 30.  Those
+//    multiples are 120 p apart, i.e. exactly p 32-bit words (120 numbers) with
+//    the same bit, so the inner loop is one shared atomicAnd and one add;
+//  * larger p: a lane per prime stepping q along the 30-wheel.
+// ceil(lo / p) comes from a precomputed reciprocal floor((2^64 - 1) / p) and
+// one correction step.
 #define PS_NT 512
+#define PS_SMALL 15
+#define PS_PAT 491                // 7 + 11 + ... + 61 pattern words
+#define PS_GAPS 0x26424246u       // gaps between consecutive wheel offsets, a nibble each
 struct PsArgs {
   uint64_t x_lo, x_hi;
   int64_t lo0;           // first segment start (multiple of 240)
   int64_t end;           // sieve [lo0, end)
-  int64_t seg;           // numbers per segment = PS_WORDS * 240
+  int64_t seg;           // numbers per segment = words * 240
   int64_t nseg;
   int64_t qlo, qhi;      // B queries: primes p in (qlo, qhi]
   int32_t mode;          // 0 count, 1 B
-  int32_t nbase;
-  const uint32_t* base;  // primes >= 7 up to sqrt(end)
+  int32_t words;         // 64-bit words per segment (a multiple of 4096, at most 16384)
+  int32_t nbase;         // primes >= 67 up to sqrt(end)
+  int32_t nmid;          // base[0, nmid) crossed off a warp per prime
+  const uint32_t* base;
+  const uint64_t* magic; // floor((2^64 - 1) / base[k])
   const uint64_t* pibig; // PiTable bits for the B queries
   int64_t* seg_c;
   int64_t* seg_m;
@@ -369,17 +384,47 @@ struct PsArgs {
   int* queue;
 };
 
-__global__ void __launch_bounds__(PS_NT) k_psieve(const PsArgs A)
+static __device__ __forceinline__ uint64_t ceil_div_magic(uint64_t n, uint32_t p, uint64_t m)
 {
+  uint64_t q = __umul64hi(n, m);     // floor(n / p) or one less
+  if (n - q * p >= p) q++;
+  return q + (q * p != n);
+}
+
+__constant__ uint32_t c_ps_small[PS_SMALL] = {7, 11, 13, 17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61};
+
+__global__ void __launch_bounds__(PS_NT, 2) k_psieve(const PsArgs A)
+{
+  constexpr uint32_t SP[PS_SMALL] = {7, 11, 13, 17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61};
   extern __shared__ __align__(16) unsigned char psm[];
+  const int words = A.words;
   uint64_t* bits = (uint64_t*) psm;
-  uint32_t* pref = (uint32_t*) (bits + PS_WORDS);       // PS_WORDS / 8 chunk prefixes
+  uint32_t* bits32 = (uint32_t*) psm;
+  uint32_t* pref = (uint32_t*) (bits + words);           // words / 8 chunk prefixes
+  uint64_t* pat = (uint64_t*) (pref + words / 8);        // wheel patterns of 7..61
+  __shared__ uint8_t s_bit[120];                         // bit of residue r in a 32-bit word
   __shared__ int s_s;
   __shared__ uint32_t wt[32];
   __shared__ long long red[3][32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int nch = PS_WORDS / 8;
+  const int nch = words / 8;
   const u128 x = ((u128) A.x_hi << 64) | A.x_lo;
+  for (int i = tid; i < 120; i += PS_NT) s_bit[i] = (uint8_t) bit_of((uint32_t) i);
+  for (int i = tid; i < PS_PAT; i += PS_NT) {
+    int k = 0, b0 = 0;
+    while (i >= b0 + (int) c_ps_small[k]) { b0 += c_ps_small[k]; k++; }
+    const uint32_t p = c_ps_small[k], r = (uint32_t) (i - b0);
+    uint64_t v = 0;
+    for (int b = 0; b < 64; b++) {
+      const uint32_t n = 240u * r + 30u * (b >> 3) + woff(b & 7);
+      if (n % p) v |= 1ull << b;
+    }
+    pat[i] = v;
+  }
+  uint64_t small_mask = 0;                               // 7..61 in word 0
+#pragma unroll
+  for (int i = 0; i < PS_SMALL; i++) small_mask |= 1ull << bit_of(SP[i]);
+  const uint32_t lane_res = 30u * (uint32_t) (lane >> 3) + woff((uint32_t) lane & 7);
   for (;;) {
     __syncthreads();
     if (tid == 0) s_s = atomicAdd(A.queue, 1);
@@ -390,45 +435,68 @@ __global__ void __launch_bounds__(PS_NT) k_psieve(const PsArgs A)
     const uint64_t hi = (uint64_t) dmin((int64_t) lo + A.seg, A.end);
     const uint32_t span = (uint32_t) (hi - lo);
     const int wused = (int) ((span + 239) / 240);
-    for (int w = tid; w < PS_WORDS; w += PS_NT) {
-      uint64_t v = w < wused ? ~0ull : 0ull;
-      if (w == wused - 1) v &= mask_le((span - 1) % 240);
-      if (lo == 0 && w == 0) v &= ~1ull;        // 1 is not prime
-      bits[w] = v;
-    }
-    __syncthreads();
-    // cross off p * q, q >= p, q coprime to 30: a warp per prime for small p,
-    // a lane per prime for large ones
-    for (int k = warp; k < A.nbase; k += PS_NT / 32) {
-      const uint64_t p = A.base[k];
-      if (p * p >= hi) break;
-      if (p >= 4096) break;
-      uint64_t qlo = (lo + p - 1) / p;
-      if (qlo < p) qlo = p;
-      const uint64_t qhi = (hi - 1) / p;
-      if (qlo > qhi) continue;
-      const uint64_t jlo = cnt_le(qlo - 1), jhi = cnt_le(qhi);
-      for (uint64_t j = jlo + lane; j < jhi; j += 32) {
-        const uint64_t q = 30 * (j >> 3) + woff((uint32_t) (j & 7));
-        const uint32_t off = (uint32_t) (p * q - lo);
-        const uint32_t w = off / 240, r = off - w * 240;
-        atomicAnd((unsigned long long*) &bits[w], ~(1ull << bit_of(r)));
+    const uint32_t nw32 = (span + 119) / 120;
+    {
+      // pattern phases of this thread's first word, advanced by PS_NT words per step
+      const uint64_t g0 = lo / 240 + (uint64_t) tid;
+      uint32_t ph[PS_SMALL];
+#pragma unroll
+      for (int i = 0; i < PS_SMALL; i++) ph[i] = (uint32_t) (g0 % SP[i]);
+      for (int w = tid; w < words; w += PS_NT) {
+        uint64_t v = 0;
+        if (w < wused) {
+          v = ~0ull;
+          uint32_t po = 0;
+#pragma unroll
+          for (int i = 0; i < PS_SMALL; i++) {
+            v &= pat[po + ph[i]];
+            po += SP[i];
+          }
+          if (lo == 0 && w == 0) v = (v | small_mask) & ~1ull;   // 7..61 are prime, 1 is not
+          if (w == wused - 1) v &= mask_le((span - 1) % 240);
+        }
+        bits[w] = v;
+#pragma unroll
+        for (int i = 0; i < PS_SMALL; i++) {
+          ph[i] += PS_NT % SP[i];
+          if (ph[i] >= SP[i]) ph[i] -= SP[i];
+        }
       }
     }
-    for (int k = tid; k < A.nbase; k += PS_NT) {
-      const uint64_t p = A.base[k];
-      if (p < 4096) continue;
-      if (p * p >= hi) break;
-      uint64_t qlo = (lo + p - 1) / p;
-      if (qlo < p) qlo = p;
-      const uint64_t qhi = (hi - 1) / p;
-      if (qlo > qhi) continue;
-      const uint64_t jlo = cnt_le(qlo - 1), jhi = cnt_le(qhi);
-      for (uint64_t j = jlo; j < jhi; j++) {
-        const uint64_t q = 30 * (j >> 3) + woff((uint32_t) (j & 7));
-        const uint32_t off = (uint32_t) (p * q - lo);
-        const uint32_t w = off / 240, r = off - w * 240;
-        atomicAnd((unsigned long long*) &bits[w], ~(1ull << bit_of(r)));
+    __syncthreads();
+    // medium primes: a warp per prime, a residue class of q mod 120 per lane
+    for (int k = warp; k < A.nmid; k += PS_NT / 32) {
+      const uint32_t p = A.base[k];
+      if ((uint64_t) p * p >= hi) break;
+      uint64_t qmin = ceil_div_magic(lo, p, A.magic[k]);
+      if (qmin < p) qmin = p;
+      const uint32_t qm = (uint32_t) (qmin % 120);
+      const uint64_t q = qmin + (lane_res >= qm ? lane_res - qm : lane_res + 120 - qm);
+      const uint64_t pq = (uint64_t) p * q;
+      if (pq < hi) {
+        const uint32_t off = (uint32_t) (pq - lo);
+        uint32_t w = off / 120;
+        const uint32_t msk = ~(1u << s_bit[off - 120 * w]);
+        for (; w < nw32; w += p) atomicAnd(&bits32[w], msk);
+      }
+    }
+    // large primes: a lane per prime along the 30-wheel
+    for (int k = A.nmid + tid; k < A.nbase; k += PS_NT) {
+      const uint32_t p = A.base[k];
+      if ((uint64_t) p * p >= hi) break;
+      uint64_t qmin = ceil_div_magic(lo, p, A.magic[k]);
+      if (qmin < p) qmin = p;
+      const uint64_t j = cnt_le(qmin - 1);              // wheel index of the first q >= qmin
+      const uint64_t q = 30 * (j >> 3) + woff((uint32_t) (j & 7));
+      const uint64_t pq = (uint64_t) p * q;
+      if (pq >= hi) continue;
+      uint32_t off = (uint32_t) (pq - lo);
+      uint32_t jj = (uint32_t) (j & 7);
+      while (off < span) {
+        const uint32_t w = off / 120;
+        atomicAnd(&bits32[w], ~(1u << s_bit[off - 120 * w]));
+        off += p * ((PS_GAPS >> (4 * jj)) & 15u);
+        jj = (jj + 1) & 7;
       }
     }
     __syncthreads();
@@ -438,9 +506,11 @@ __global__ void __launch_bounds__(PS_NT) k_psieve(const PsArgs A)
       const int base = tid * cpt;
       uint32_t loc[4];
       uint32_t sum = 0;
-      for (int c = 0; c < cpt; c++) {
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
         uint32_t t = 0;
-        for (int i = 0; i < 8; i++) t += __popcll(bits[8 * (base + c) + i]);
+        if (c < cpt)
+          for (int i = 0; i < 8; i++) t += __popcll(bits[8 * (base + c) + i]);
         loc[c] = t;
         sum += t;
       }
@@ -453,7 +523,9 @@ __global__ void __launch_bounds__(PS_NT) k_psieve(const PsArgs A)
       __syncthreads();
       uint32_t run = incl - sum;
       for (int w = 0; w < warp; w++) run += wt[w];
-      for (int c = 0; c < cpt; c++) { pref[base + c] = run; run += loc[c]; }
+#pragma unroll
+      for (int c = 0; c < 4; c++)
+        if (c < cpt) { pref[base + c] = run; run += loc[c]; }
       if (tid == PS_NT - 1 && A.seg_c) A.seg_c[s] = run;
       __syncthreads();
     }
@@ -498,13 +570,14 @@ __global__ void __launch_bounds__(PS_NT) k_psieve(const PsArgs A)
   }
 }
 
-static std::vector<uint32_t> base_primes7(int64_t limit)
+// primes 67 <= p <= limit (the sieve's cross-off primes above the patterns)
+static std::vector<uint32_t> base_primes67(int64_t limit)
 {
-  std::vector<uint8_t> c((size_t) limit + 1, 0);
+  std::vector<uint8_t> c((size_t) std::max<int64_t>(limit, 1) + 1, 0);
   std::vector<uint32_t> p;
   for (int64_t i = 2; i <= limit; i++) {
     if (c[(size_t) i]) continue;
-    if (i >= 7) p.push_back((uint32_t) i);
+    if (i >= 67) p.push_back((uint32_t) i);
     for (int64_t m = i * i; m <= limit; m += i) c[(size_t) m] = 1;
   }
   return p;
@@ -515,6 +588,28 @@ struct PsOut {
   int64_t lo0 = 0, nseg = 0;
 };
 
+// segment words and the warp/lane split of the prime sieve (PCG_PS_WORDS,
+// PCG_PS_MID override them; words must be 4096, 8192, 12288 or 16384)
+static int ps_words()
+{
+  static const int w = [] {
+    const char* e = getenv("PCG_PS_WORDS");
+    const int v = e ? atoi(e) : 12288;
+    return (v >= 4096 && v <= 16384 && v % 4096 == 0) ? v : 12288;
+  }();
+  return w;
+}
+
+static int64_t ps_mid_div()
+{
+  static const int64_t d = [] {
+    const char* e = getenv("PCG_PS_MID");
+    const int64_t v = e ? atoll(e) : 512;
+    return v > 0 ? v : 512;
+  }();
+  return d;
+}
+
 // sieve [lo0, end) in segments; B queries for primes in (qlo, qhi] when b_mode
 static PsOut run_psieve(Ctx& c, u128 x, int64_t lo0, int64_t end, bool b_mode, int64_t qlo, int64_t qhi,
                         cudaStream_t s, uint64_t* launches)
@@ -522,17 +617,29 @@ static PsOut run_psieve(Ctx& c, u128 x, int64_t lo0, int64_t end, bool b_mode, i
   PsOut o;
   lo0 -= lo0 % 240;
   o.lo0 = lo0;
-  const int64_t seg = (int64_t) PS_WORDS * 240;
+  const int words = ps_words();
+  const int64_t seg = (int64_t) words * 240;
   o.nseg = (end - lo0 + seg - 1) / seg;
   if (o.nseg <= 0) return o;
-  std::vector<uint32_t> base = base_primes7(isqrt((u128) end) + 1);
-  DevBuf d_base, d_c, d_m, d_l, d_q;
+  std::vector<uint32_t> base = base_primes67(isqrt((u128) end) + 1);
+  std::vector<uint64_t> magic(base.size());
+  int nmid = 0;
+  const int64_t mid_limit = seg / ps_mid_div();
+  for (size_t i = 0; i < base.size(); i++) {
+    magic[i] = UINT64_MAX / base[i];
+    if ((int64_t) base[i] < mid_limit) nmid = (int) i + 1;
+  }
+  DevBuf d_base, d_magic, d_c, d_m, d_l, d_q;
   d_base.alloc(std::max<size_t>(base.size(), 1) * 4);
+  d_magic.alloc(std::max<size_t>(base.size(), 1) * 8);
   d_c.alloc((size_t) o.nseg * 8);
   d_m.alloc((size_t) o.nseg * 8);
   d_l.alloc((size_t) o.nseg * 8);
   d_q.alloc(64);
-  if (!base.empty()) PCG_CUDA(cudaMemcpyAsync(d_base.p, base.data(), base.size() * 4, cudaMemcpyHostToDevice, s));
+  if (!base.empty()) {
+    PCG_CUDA(cudaMemcpyAsync(d_base.p, base.data(), base.size() * 4, cudaMemcpyHostToDevice, s));
+    PCG_CUDA(cudaMemcpyAsync(d_magic.p, magic.data(), magic.size() * 8, cudaMemcpyHostToDevice, s));
+  }
   PCG_CUDA(cudaMemsetAsync(d_q.p, 0, 64, s));
   PCG_CUDA(cudaMemsetAsync(d_m.p, 0, (size_t) o.nseg * 8, s));
   PCG_CUDA(cudaMemsetAsync(d_l.p, 0, (size_t) o.nseg * 8, s));
@@ -547,19 +654,18 @@ static PsOut run_psieve(Ctx& c, u128 x, int64_t lo0, int64_t end, bool b_mode, i
   a.qlo = qlo;
   a.qhi = qhi;
   a.mode = b_mode ? 1 : 0;
+  a.words = words;
   a.nbase = (int) base.size();
+  a.nmid = nmid;
   a.base = d_base.as<uint32_t>();
+  a.magic = d_magic.as<uint64_t>();
   a.pibig = c.tab.pibig.as<uint64_t>();
   a.seg_c = d_c.as<int64_t>();
   a.seg_m = d_m.as<int64_t>();
   a.seg_l = d_l.as<int64_t>();
   a.queue = d_q.as<int>();
-  const size_t smem = (size_t) PS_WORDS * 8 + (PS_WORDS / 8) * 4;
-  static bool attr = false;
-  if (!attr) {
-    PCG_CUDA(cudaFuncSetAttribute(k_psieve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
-    attr = true;
-  }
+  const size_t smem = (size_t) words * 8 + (size_t) (words / 8) * 4 + PS_PAT * 8;
+  PCG_CUDA(cudaFuncSetAttribute(k_psieve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
   int occ = 0;
   PCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_psieve, PS_NT, smem));
   const int grid = (int) std::min<int64_t>((int64_t) c.num_sms * std::max(occ, 1), o.nseg);
