@@ -75,4 +75,13 @@ static __device__ __forceinline__ u128 div128(u128 a, uint64_t d)
 }
 
 
+// floor(n / q) from m = floor((2^64 - 1) / q), q >= 1: the high product is
+// floor(n / q) or one less
+static __device__ __forceinline__ uint64_t div_magic(uint64_t n, uint64_t q, uint64_t m)
+{
+  uint64_t t = __umul64hi(n, m);
+  if (n - t * q >= q) t++;
+  return t;
+}
+
 }  // namespace pcg

@@ -168,25 +168,63 @@ struct PairOuter {
   int32_t mode;
 };
 
+// pi(n) for n >= 6 from the PiTable {count, bits} per 240 numbers (the
+// count of a word includes 2, 3 and 5); s_mask[r] = bits of numbers <= r.
+// Below 2^36 the word index is a 32-bit division: n / 240 = (n / 16) / 15.
+static __device__ __forceinline__ long long pi_pt(const ulonglong2* __restrict__ pt, const uint64_t* s_mask,
+                                                  uint64_t n)
+{
+  uint64_t w;
+  uint32_t r;
+  if ((n >> 36) == 0) {
+    const uint32_t w32 = (uint32_t) (n >> 4) / 15u;
+    w = w32;
+    r = (uint32_t) n - 240u * w32;                   // exact modulo 2^32
+  } else {
+    w = n / 240;
+    r = (uint32_t) (n - 240 * w);
+  }
+  const ulonglong2 e = pt[w];
+  return (long long) e.x + __popcll(e.y & s_mask[r]);
+}
+
+template <int MODE>
+__device__ __forceinline__ long long pair_terms(const PairOuter& O, const uint32_t* __restrict__ primes,
+                                                const uint64_t* __restrict__ magic,
+                                                const ulonglong2* __restrict__ pt, const uint64_t* s_mask)
+{
+  long long s = 0;
+  for (int64_t i = O.i_lo + 1 + threadIdx.x; i <= O.i_hi; i += blockDim.x) {
+    const uint32_t q = primes[i];
+    uint64_t n;
+    if (O.xp_hi == 0) n = div_magic(O.xp_lo, q, magic[i]);
+    else n = (uint64_t) ((((u128) O.xp_hi << 64) | O.xp_lo) / q);
+    const long long pin = n < 6 ? (long long) ((0x322100u >> (4 * n)) & 15u) : pi_pt(pt, s_mask, n);
+    if (MODE == 0) s += (q <= O.cap) ? pin : 2 * pin;
+    else if (MODE == 1) s += pin - O.b + 2;
+    else if (MODE == 2) s -= pin - O.b + 2;
+    else s += pin - i + 1;
+  }
+  return s;
+}
+
 __global__ void __launch_bounds__(256) k_pairs(const PairOuter* __restrict__ outs, int64_t n_outer,
                                                const uint32_t* __restrict__ primes,
+                                               const uint64_t* __restrict__ magic,
                                                const uint64_t* __restrict__ pibig, i128* __restrict__ partial)
 {
+  __shared__ uint64_t s_mask[240];
+  for (int r = threadIdx.x; r < 240; r += blockDim.x) s_mask[r] = mask_le((uint32_t) r);
+  __syncthreads();
+  const ulonglong2* __restrict__ pt = (const ulonglong2*) pibig;
   i128 acc = 0;
   for (int64_t o = blockIdx.x; o < n_outer; o += gridDim.x) {
     const PairOuter O = outs[o];
-    long long s = 0;
-    for (int64_t i = O.i_lo + 1 + threadIdx.x; i <= O.i_hi; i += blockDim.x) {
-      const uint64_t q = primes[i];
-      uint64_t n;
-      if (O.xp_hi == 0) n = O.xp_lo / q;
-      else n = (uint64_t) ((((u128) O.xp_hi << 64) | O.xp_lo) / q);
-      const long long pin = dpi(pibig, n);
-      if (O.mode == 0) s += (q <= O.cap) ? pin : 2 * pin;
-      else if (O.mode == 1) s += pin - O.b + 2;
-      else if (O.mode == 2) s -= pin - O.b + 2;
-      else s += pin - i + 1;
-    }
+    long long s;
+    if (O.mode == 0) s = pair_terms<0>(O, primes, magic, pt, s_mask);
+    else if (O.mode == 1) s = pair_terms<1>(O, primes, magic, pt, s_mask);
+    else if (O.mode == 2) s = pair_terms<2>(O, primes, magic, pt, s_mask);
+    else s = pair_terms<3>(O, primes, magic, pt, s_mask);
     acc += s;
   }
   block_sum_i128<256>(acc, &partial[blockIdx.x]);
@@ -828,7 +866,7 @@ static PiParts pi_gourdon(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s)
       DevBuf part;
       part.alloc((size_t) grid * 16);
       PCG_CUDA(cudaMemsetAsync(part.p, 0, (size_t) grid * 16, s));
-      k_pairs<<<grid, 256, 0, s>>>(o, nout, T.primes.as<uint32_t>(), T.pibig.as<uint64_t>(), part.as<i128>());
+      k_pairs<<<grid, 256, 0, s>>>(o, nout, T.primes.as<uint32_t>(), c.tab.pmagic.as<uint64_t>(), T.pibig.as<uint64_t>(), part.as<i128>());
       PCG_CUDA(cudaGetLastError());
       R.launches++;
       sum = sum_partials(part, grid, s);
@@ -1056,7 +1094,7 @@ int64_t phi_any(Ctx& c, int64_t x, int64_t a, const Tuning& tune, cudaStream_t s
       const int grid = (int) std::min<int64_t>(n, (int64_t) c.num_sms * 8);
       part.alloc((size_t) grid * 16);
       PCG_CUDA(cudaMemsetAsync(part.p, 0, (size_t) grid * 16, s));
-      k_pairs<<<grid, 256, 0, s>>>(outs.as<PairOuter>(), n, c.tab.primes.as<uint32_t>(), c.tab.pibig.as<uint64_t>(),
+      k_pairs<<<grid, 256, 0, s>>>(outs.as<PairOuter>(), n, c.tab.primes.as<uint32_t>(), c.tab.pmagic.as<uint64_t>(), c.tab.pibig.as<uint64_t>(),
                                    part.as<i128>());
       PCG_CUDA(cudaGetLastError());
       P3 = sum_partials(part, grid, s);

@@ -72,6 +72,7 @@ struct Tables {
   int64_t prime_limit = -1;  // tables cover [0, prime_limit]
   int64_t nprimes = 0;
   DevBuf primes;             // uint32[nprimes + 2]
+  DevBuf pmagic;             // uint64[nprimes + 2]: floor((2^64 - 1) / primes[i])
   DevBuf pitab;              // uint64[2 * (prime_limit / 240 + 1)]
   std::vector<uint32_t> h_primes;   // host copy of the primes (small part)
   std::vector<uint64_t> h_pitab;    // host copy of the PiTable
@@ -83,6 +84,10 @@ struct Tables {
   int64_t fr_y = -1;
   int fr_bytes = 2;
   DevBuf factor_dr;
+  // floor((2^64 - 1) / m) for the numbers m coprime to 2310, by factor-table
+  // index, for the indices [0, finv_n)
+  int64_t finv_n = 0;
+  DevBuf finv;
   // PiTable up to sqrt(x) for the A, B, C formulas of pi(x) (no primes array)
   int64_t pibig_limit = -1;
   DevBuf pibig;

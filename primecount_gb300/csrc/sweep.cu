@@ -322,6 +322,8 @@ struct SweepArgs {
   const uint64_t* xp_tab;   // [bglob+1][3]: x/p lo, hi, min(x/p^3, 2^63-1)
   const uint16_t* coprime;
   const int16_t* cindex;
+  const uint64_t* finv;      // floor((2^64 - 1) / m) by factor-table index
+  const uint64_t* pmagic;    // floor((2^64 - 1) / p) by prime index
   uint32_t* cnt;            // [wave_len][bglob+1]
   int32_t* smu;             // [wave_len][bglob+1]
   int64_t* segsum;          // [wave_len]
@@ -352,28 +354,52 @@ __device__ __forceinline__ uint64_t div_xp(uint64_t xlo, uint64_t xhi, uint64_t 
   return (uint64_t) (xp / m);
 }
 
+// exclusive prefix of the chunk counts (nch / (NT / 32) chunks per warp, a
+// multiple of 32; ccount and pref 16-byte aligned).  Each warp scans its own
+// range and adds the total of the chunks before it, which it reads itself, so
+// no warp waits for another before the single closing barrier.
 template <int NT>
-__device__ __forceinline__ void block_scan_chunks(const uint32_t* __restrict__ ccount, uint32_t* __restrict__ pref,
-                                                  int nch, uint32_t* wtmp)
+__device__ __forceinline__ void scan_chunks(const uint32_t* __restrict__ ccount, uint32_t* __restrict__ pref, int nch)
 {
-  // exclusive prefix of the chunk counts; two barriers: warp totals, then the result
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int cpt = nch / NT;      // nch is a multiple of NT
-  const int base = tid * cpt;
-  uint32_t s = 0;
-  for (int c = 0; c < cpt; c++) s += ccount[base + c];
-  uint32_t incl = s;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int cpw = nch / (NT / 32);
+  const int cpl = cpw >> 5;
+  const int base = warp * cpw;
+  const uint4* c4 = (const uint4*) ccount;
+  uint32_t before = 0;
+  for (int i = lane; 4 * i < base; i += 32) {
+    const uint4 v = c4[i];
+    before += v.x + v.y + v.z + v.w;
+  }
+  before = __reduce_add_sync(0xffffffffu, before);
+  const int my = base + lane * cpl;
+  uint32_t sum = 0;
+  if ((cpl & 3) == 0) {
+    for (int i = 0; i < cpl; i += 4) {
+      const uint4 v = *(const uint4*) (ccount + my + i);
+      sum += v.x + v.y + v.z + v.w;
+    }
+  } else {
+    for (int i = 0; i < cpl; i++) sum += ccount[my + i];
+  }
+  uint32_t incl = sum;
   for (int d = 1; d < 32; d <<= 1) {
-    uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
+    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
     if (lane >= d) incl += t;
   }
-  if (lane == 31) wtmp[warp] = incl;
-  __syncthreads();
-  uint32_t run = incl - s;
-  for (int w = 0; w < warp; w++) run += wtmp[w];
-  for (int c = 0; c < cpt; c++) {
-    pref[base + c] = run;
-    run += ccount[base + c];
+  uint32_t run = before + incl - sum;
+  if ((cpl & 3) == 0) {
+    for (int i = 0; i < cpl; i += 4) {
+      const uint4 v = *(const uint4*) (ccount + my + i);
+      uint4 o;
+      o.x = run; run += v.x;
+      o.y = run; run += v.y;
+      o.z = run; run += v.z;
+      o.w = run; run += v.w;
+      *(uint4*) (pref + my + i) = o;
+    }
+  } else {
+    for (int i = 0; i < cpl; i++) { pref[my + i] = run; run += ccount[my + i]; }
   }
   __syncthreads();
 }
@@ -393,19 +419,27 @@ __device__ __forceinline__ uint32_t query(const uint64_t* __restrict__ bits, con
 // Record of one table entry: the offset of the leaf in the segment, bit 30 =
 // negative sign, or REC_NONE when the factor-table filter rejects the entry.
 #define REC_NONE 0xFFFFFFFFu
+// x / (p m) through the reciprocal of m when x / p < 2^64
 template <typename FT>
 __device__ __forceinline__ uint32_t make_record(const SweepArgs& A, const LevelP& P, int64_t e, uint32_t fv,
                                                 const uint16_t* __restrict__ cop, uint64_t low)
 {
   const uint64_t* xt = A.xp_tab + 3 * (int64_t) P.level;
+  const uint64_t xlo = xt[0], xhi = xt[1];
+  const int64_t idx = P.hi - e;
   if (!(P.flags & 2)) {
     if (fv <= P.thr) return REC_NONE;
-    const uint64_t mi = (uint64_t) (P.hi - e);
-    const uint64_t m = 2310 * (mi / 480) + cop[mi % 480];
-    const uint64_t nn = div_xp(xt[0], xt[1], m);
+    uint64_t m;
+    if ((uint64_t) idx <= 0xFFFFFFFFull) {
+      const uint32_t mi = (uint32_t) idx;
+      m = 2310ull * (mi / 480u) + cop[mi % 480u];
+    } else {
+      m = 2310ull * ((uint64_t) idx / 480) + cop[(uint64_t) idx % 480];
+    }
+    const uint64_t nn = xhi == 0 ? div_magic(xlo, m, __ldg(&A.finv[idx])) : div_xp(xlo, xhi, m);
     return (uint32_t) (nn - low) | ((fv & 1) ? 0u : (1u << 30));
   }
-  const uint64_t nn = div_xp(xt[0], xt[1], (uint64_t) fv);
+  const uint64_t nn = xhi == 0 ? div_magic(xlo, fv, __ldg(&A.pmagic[idx])) : div_xp(xlo, xhi, (uint64_t) fv);
   return (uint32_t) (nn - low);
 }
 
@@ -431,7 +465,7 @@ __device__ __forceinline__ void block_scan3(long long v0, long long v1, long lon
 }
 
 template <typename FT, int NT>
-__global__ void __launch_bounds__(NT, (NT >= 512) ? 2 : ((NT >= 256) ? 3 : 4)) k_sweep(const SweepArgs A)
+__global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k_sweep(const SweepArgs A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nch = A.words >> 3;
@@ -440,7 +474,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 2 : ((NT >= 256) ? 3 : 4)) k
   int64_t* loff = (int64_t*) (pat + PAT_WORDS);        // record offsets of the batch levels
   int64_t* hoff = loff + (NT + 1);                     // cross-off co-factor offsets
   int64_t* rpre = hoff + (NT + 1);                     // prefix of the formula counts
-  uint32_t* ccount = (uint32_t*) (rpre + (NT + 1));
+  uint32_t* ccount = (uint32_t*) (((uintptr_t) (rpre + (NT + 1)) + 15) & ~(uintptr_t) 15);  // 16-byte aligned
   uint32_t* pref = ccount + nch;
   LevelP* lp = (LevelP*) (pref + nch);
   uint32_t* rec = (uint32_t*) (lp + NT);
@@ -452,7 +486,6 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 2 : ((NT >= 256) ? 3 : 4)) k
   __shared__ int s_stop;
   __shared__ uint32_t s_rem[3];
   __shared__ uint32_t s_total;
-  __shared__ uint32_t wtmp[32];
   __shared__ long long wt3[32][3];
   __shared__ int s_brk[32];
   __shared__ long long s_red[NT / 32];
@@ -664,6 +697,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 2 : ((NT >= 256) ? 3 : 4)) k
         // ---- phase A: the window's leaf records (flat over levels, 4 loads in flight)
         const int nrec = (int) dmax(0, dmin(wend, total_e) - w0);
         if (nrec > 0) {
+          int lv = li;       // level of this thread's previous entry
           for (int f0 = tid; f0 < nrec; f0 += 4 * NT) {
             int jl[4];
             int64_t el[4];
@@ -674,11 +708,19 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 2 : ((NT >= 256) ? 3 : 4)) k
               jl[u] = -1;
               if (f < nrec) {
                 const int64_t pos = w0 + f;
-                int lo = li, hi = nb - 1;     // last level with loff <= pos
-                while (lo < hi) {
-                  const int mid = (lo + hi + 1) >> 1;
-                  if (loff[mid] <= pos) lo = mid; else hi = mid - 1;
+                // last level with loff <= pos: a few steps forward from the
+                // previous entry's level, else a binary search
+                int lo = lv;
+                int steps = 0;
+                while (lo + 1 < nb && loff[lo + 1] <= pos && steps < 4) { lo++; steps++; }
+                if (lo + 1 < nb && loff[lo + 1] <= pos) {
+                  int hi = nb - 1;
+                  while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (loff[mid] <= pos) lo = mid; else hi = mid - 1;
+                  }
                 }
+                lv = lo;
                 jl[u] = lo;
                 el[u] = pos - loff[lo];
                 const LevelP& Q = lp[lo];
@@ -743,7 +785,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 2 : ((NT >= 256) ? 3 : 4)) k
           if (la >= w0 && tid == 0) A.cnt[(int64_t) ws * cols + l] = total;
           const int ra = (int) (dmax(la, w0) - w0), rb = (int) (dmin(lz, wend) - w0);
           if (rb > ra) {
-            if (dirty) { block_scan_chunks<NT>(ccount, pref, nch, wtmp); dirty = false; }
+            if (dirty) { scan_chunks<NT>(ccount, pref, nch); dirty = false; }
             if (ra + 32 * warp < rb) {
               int smu_t = 0;
               for (int k2 = ra + tid; k2 < rb; k2 += NT) {
@@ -956,6 +998,26 @@ int64_t host_pi(const Tables& t, uint64_t x)
   return (int64_t) (t.h_pitab[2 * i] + (uint64_t) __builtin_popcountll(t.h_pitab[2 * i + 1] & m));
 }
 
+// floor((2^64 - 1) / p) for the primes p = primes[1 .. n]: x / p then costs a
+// 64x64 high multiply and one correction step (the reference divides by
+// libdivide's precomputed reciprocals for the same reason)
+__global__ void k_prime_magic(const uint32_t* __restrict__ primes, int64_t n, uint64_t* __restrict__ magic)
+{
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < 1 || i > n) return;
+  magic[i] = UINT64_MAX / primes[i];
+}
+
+// floor((2^64 - 1) / m) for the numbers m coprime to 2310 with factor-table
+// index in [0, n)
+__global__ void k_factor_inv(const uint16_t* __restrict__ cop, int64_t n, uint64_t* __restrict__ inv)
+{
+  const int64_t i = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint64_t m = 2310 * (uint64_t) (i / 480) + cop[i % 480];
+  inv[i] = UINT64_MAX / m;
+}
+
 void ensure_prime_tables(Ctx& c, int64_t limit, cudaStream_t s)
 {
   Tables& t = c.tab;
@@ -998,6 +1060,9 @@ void ensure_prime_tables(Ctx& c, int64_t limit, cudaStream_t s)
   PCG_CUDA(cudaMemcpyAsync(t.primes.p, head, sizeof(head), cudaMemcpyHostToDevice, s));
   k_pitab_primes<<<(unsigned) ((nwords + 255) / 256), 256, 0, s>>>(d_bits.as<uint64_t>(), d_excl.as<uint64_t>(), nwords,
                                                                    t.pitab.as<uint64_t>(), t.primes.as<uint32_t>());
+  t.pmagic.alloc((size_t) (np + 2) * 8);
+  PCG_CUDA(cudaMemsetAsync(t.pmagic.p, 0, (size_t) (np + 2) * 8, s));
+  k_prime_magic<<<(unsigned) ((np + 256) / 256), 256, 0, s>>>(t.primes.as<uint32_t>(), np, t.pmagic.as<uint64_t>());
   PCG_CUDA(cudaGetLastError());
   t.h_pitab.resize((size_t) nwords * 2);
   PCG_CUDA(cudaMemcpyAsync(t.h_pitab.data(), t.pitab.p, (size_t) nwords * 16, cudaMemcpyDeviceToHost, s));
@@ -1085,6 +1150,17 @@ static void build_factor(Ctx& c, DevBuf& out, int64_t limit, int64_t y, int gour
   }
 }
 
+// reciprocals of the factor-table numbers for the indices [0, n)
+static void ensure_finv(Ctx& c, int64_t n, cudaStream_t s)
+{
+  Tables& t = c.tab;
+  if (t.finv_n >= n) return;
+  t.finv.alloc((size_t) n * 8);
+  k_factor_inv<<<(unsigned) ((n + 255) / 256), 256, 0, s>>>(t.coprime.as<uint16_t>(), n, t.finv.as<uint64_t>());
+  PCG_CUDA(cudaGetLastError());
+  t.finv_n = n;
+}
+
 void ensure_factor_d(Ctx& c, int64_t y, int64_t z, cudaStream_t s)
 {
   Tables& t = c.tab;
@@ -1096,6 +1172,7 @@ void ensure_factor_d(Ctx& c, int64_t y, int64_t z, cudaStream_t s)
   t.fd_bytes = (z <= 386083ll * 386083 - 1) ? 2 : 4;
   if (t.fd_bytes == 2) build_factor<uint16_t>(c, t.factor_d, z, y, 1, s);
   else build_factor<uint32_t>(c, t.factor_d, z, y, 1, s);
+  ensure_finv(c, wheel2310().to_index((uint64_t) std::max<int64_t>(z, 1)) + 1, s);
   PCG_CUDA(cudaStreamSynchronize(s));
   t.fd_y = y;
   t.fd_z = z;
@@ -1111,6 +1188,7 @@ void ensure_factor_dr(Ctx& c, int64_t y, cudaStream_t s)
   t.fr_bytes = (y <= 65534ll * 65534 - 1) ? 2 : 4;
   if (t.fr_bytes == 2) build_factor<uint16_t>(c, t.factor_dr, y, y, 0, s);
   else build_factor<uint32_t>(c, t.factor_dr, y, y, 0, s);
+  ensure_finv(c, wheel2310().to_index((uint64_t) std::max<int64_t>(y, 1)) + 1, s);
   PCG_CUDA(cudaStreamSynchronize(s));
   t.fr_y = y;
   t.build_ms += now_ms() - t0;
@@ -1292,7 +1370,7 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   words = (words + 8 * NT - 1) / (8 * NT) * (8 * NT);
   const int cap = 4096;
   size_t smem = (size_t) words * 8 + PAT_WORDS * 8 + (size_t) (NT + 1) * 8 * 3 + (size_t) (words / 8) * 8 +
-                sizeof(LevelP) * NT + (size_t) cap * 4 + (size_t) NT * 2 + 480 * 2 + 16;
+                sizeof(LevelP) * NT + (size_t) cap * 4 + (size_t) NT * 2 + 480 * 2 + 32;
   if (smem > c.smem_optin) fail(PCG_EINVAL, "segment too large for shared memory");
   int fbytes = pb.gourdon ? c.tab.fd_bytes : c.tab.fr_bytes;
   auto occupancy = [&](int* occ) {
@@ -1357,6 +1435,8 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   a.xp_tab = d_xp;
   a.coprime = c.tab.coprime.as<uint16_t>();
   a.cindex = c.tab.cindex.as<int16_t>();
+  a.finv = c.tab.finv.as<uint64_t>();
+  a.pmagic = c.tab.pmagic.as<uint64_t>();
   a.cnt = c.cnt.as<uint32_t>();
   a.smu = c.smu.as<int32_t>();
   a.segsum = c.segsum.as<int64_t>();
@@ -1590,7 +1670,7 @@ SweepResult run_sweep_noalloc(Ctx& c, const SweepProblem& pb, cudaStream_t s)
   const int words = 8192;
   const int cap = 4096;
   size_t smem = (size_t) words * 8 + PAT_WORDS * 8 + (size_t) (NT + 1) * 8 * 3 + (size_t) (words / 8) * 8 +
-                sizeof(LevelP) * NT + (size_t) cap * 4 + (size_t) NT * 2 + 480 * 2 + 16;
+                sizeof(LevelP) * NT + (size_t) cap * 4 + (size_t) NT * 2 + 480 * 2 + 32;
   const int fbytes = T.fd_bytes;
   int occ = 0;
   if (fbytes == 2) occupancy_sweep<uint16_t, 256>(&occ, smem);
@@ -1661,6 +1741,8 @@ SweepResult run_sweep_noalloc(Ctx& c, const SweepProblem& pb, cudaStream_t s)
   a.xp_tab = d_xp;
   a.coprime = T.coprime.as<uint16_t>();
   a.cindex = T.cindex.as<int16_t>();
+  a.finv = T.finv.as<uint64_t>();
+  a.pmagic = T.pmagic.as<uint64_t>();
   a.cnt = d_cnt;
   a.smu = d_smu;
   a.segsum = d_segsum;
