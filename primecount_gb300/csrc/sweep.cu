@@ -354,52 +354,40 @@ __device__ __forceinline__ uint64_t div_xp(uint64_t xlo, uint64_t xhi, uint64_t 
   return (uint64_t) (xp / m);
 }
 
-// exclusive prefix of the chunk counts (nch / (NT / 32) chunks per warp, a
-// multiple of 32; ccount and pref 16-byte aligned).  Each warp scans its own
-// range and adds the total of the chunks before it, which it reads itself, so
-// no warp waits for another before the single closing barrier.
-template <int NT>
-__device__ __forceinline__ void scan_chunks(const uint32_t* __restrict__ ccount, uint32_t* __restrict__ pref, int nch)
+// exclusive prefix of the chunk counts by the first SW warps (nch / SW chunks
+// per warp, a multiple of 64; ccount and pref 16-byte aligned); the other
+// warps only meet the two barriers
+#define SCAN_WARPS 4
+__device__ __forceinline__ void scan_chunks(const uint32_t* __restrict__ ccount, uint32_t* __restrict__ pref, int nch,
+                                            uint32_t* wtmp)
 {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int cpw = nch / (NT / 32);
-  const int cpl = cpw >> 5;
-  const int base = warp * cpw;
-  const uint4* c4 = (const uint4*) ccount;
-  uint32_t before = 0;
-  for (int i = lane; 4 * i < base; i += 32) {
-    const uint4 v = c4[i];
-    before += v.x + v.y + v.z + v.w;
-  }
-  before = __reduce_add_sync(0xffffffffu, before);
-  const int my = base + lane * cpl;
-  uint32_t sum = 0;
-  if ((cpl & 3) == 0) {
-    for (int i = 0; i < cpl; i += 4) {
-      const uint4 v = *(const uint4*) (ccount + my + i);
-      sum += v.x + v.y + v.z + v.w;
+  const int cpl = nch / (32 * SCAN_WARPS);             // chunks per lane, a multiple of 2
+  const int my = (warp * 32 + lane) * cpl;
+  uint32_t sum = 0, incl = 0;
+  if (warp < SCAN_WARPS) {
+    for (int i = 0; i < cpl; i += 2) {
+      const uint2 v = *(const uint2*) (ccount + my + i);
+      sum += v.x + v.y;
     }
-  } else {
-    for (int i = 0; i < cpl; i++) sum += ccount[my + i];
+    incl = sum;
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += t;
+    }
+    if (lane == 31) wtmp[warp] = incl;
   }
-  uint32_t incl = sum;
-  for (int d = 1; d < 32; d <<= 1) {
-    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
-    if (lane >= d) incl += t;
-  }
-  uint32_t run = before + incl - sum;
-  if ((cpl & 3) == 0) {
-    for (int i = 0; i < cpl; i += 4) {
-      const uint4 v = *(const uint4*) (ccount + my + i);
-      uint4 o;
+  __syncthreads();
+  if (warp < SCAN_WARPS) {
+    uint32_t run = incl - sum;
+    for (int w = 0; w < warp; w++) run += wtmp[w];
+    for (int i = 0; i < cpl; i += 2) {
+      const uint2 v = *(const uint2*) (ccount + my + i);
+      uint2 o;
       o.x = run; run += v.x;
       o.y = run; run += v.y;
-      o.z = run; run += v.z;
-      o.w = run; run += v.w;
-      *(uint4*) (pref + my + i) = o;
+      *(uint2*) (pref + my + i) = o;
     }
-  } else {
-    for (int i = 0; i < cpl; i++) { pref[my + i] = run; run += ccount[my + i]; }
   }
   __syncthreads();
 }
@@ -482,6 +470,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
   uint16_t* cop = runend + NT;
 
   __shared__ int s_ws;
+  __shared__ uint32_t wtmp[32];
   __shared__ int s_smu;
   __shared__ int s_stop;
   __shared__ uint32_t s_rem[3];
@@ -785,7 +774,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
           if (la >= w0 && tid == 0) A.cnt[(int64_t) ws * cols + l] = total;
           const int ra = (int) (dmax(la, w0) - w0), rb = (int) (dmin(lz, wend) - w0);
           if (rb > ra) {
-            if (dirty) { scan_chunks<NT>(ccount, pref, nch); dirty = false; }
+            if (dirty) { scan_chunks(ccount, pref, nch, wtmp); dirty = false; }
             if (ra + 32 * warp < rb) {
               int smu_t = 0;
               for (int k2 = ra + tid; k2 < rb; k2 += NT) {
@@ -830,14 +819,17 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
               if (r >= p) r -= p;
             }
           } else if (P.jn) {
-            if (32 * warp < (int) P.jn) {
+            if ((uint32_t) tid < P.jn) {
+              // co-factors tid, tid + NT, ...: NT / 8 wheel turns apart, so
+              // the multiples are NT p / 64 words apart with the same bit
               const uint64_t p = P.prime;
-              for (uint32_t j = tid; j < P.jn; j += NT) {
-                const uint64_t jj = P.jlo + j;
-                const uint64_t q = 30 * (jj >> 3) + woff((uint32_t) (jj & 7));
-                const uint32_t off = (uint32_t) (p * q - (uint64_t) low);
-                const uint32_t w = off / 240, rr = off - w * 240;
-                const uint64_t m = 1ull << bit_of(rr);
+              const uint64_t jj = P.jlo + (uint64_t) tid;
+              const uint64_t q = 30 * (jj >> 3) + woff((uint32_t) (jj & 7));
+              const uint32_t off = (uint32_t) (p * q - (uint64_t) low);
+              uint32_t w = off / 240;
+              const uint64_t m = 1ull << bit_of(off - w * 240);
+              const uint32_t wstep = (uint32_t) p * (NT / 64);
+              for (uint32_t j = tid; j < P.jn; j += NT, w += wstep) {
                 const uint64_t old = atomicAnd((unsigned long long*) &bits[w], ~m);
                 if (old & m) { rem++; atomicSub(&ccount[w >> 3], 1u); }
               }
@@ -1366,8 +1358,9 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   // resident CTAs per SM
   const int NT = (tune.cta_threads == 512 || tune.cta_threads == 128) ? tune.cta_threads : 256;
   int words = tune.segment_words > 0 ? tune.segment_words : 8192;
-  words = std::max(words, 8 * NT);
-  words = (words + 8 * NT - 1) / (8 * NT) * (8 * NT);
+  const int wq = std::max(8 * NT, 2048);   // whole chunks per thread and per scan lane pair
+  words = std::max(words, wq);
+  words = (words + wq - 1) / wq * wq;
   const int cap = 4096;
   size_t smem = (size_t) words * 8 + PAT_WORDS * 8 + (size_t) (NT + 1) * 8 * 3 + (size_t) (words / 8) * 8 +
                 sizeof(LevelP) * NT + (size_t) cap * 4 + (size_t) NT * 2 + 480 * 2 + 32;
