@@ -13,13 +13,18 @@ e2e          the C-ABI call pcg_D on a fresh context: table construction,
              result copy, host wall clock.
 roofline     the sieve/leaf kernel (k_sweep): algorithmic table bytes
              (2 B per FactorTable entry read, 4 B per two-prime leaf,
-             16 B per (segment, b) PiTable/level step) over its launch time.
+             8 B per leaf for the divisor's reciprocal, 16 B per
+             (segment, b) PiTable/level step) over its launch time; traffic
+             = DRAM bytes per launch from the committed ncu capture.
 cpu_baseline the oracle's restatement of the reference's chunk loop on this
              host's cores, timed on an evenly spread sample of the same
              interval and scaled to the whole interval.
 
 --impl reference: the CPU reference arm (the oracle port, all host threads).
---gpus N > 1: replicas only -- each rank evaluates its own D(1e20).
+--gpus N > 1 (torchrun, NCCL): one D(1e20) over N GPUs -- rank r sweeps
+             shard r of the segment plan (pcg_D_shard), then one all-gather
+             of the per-level partials and the exact combine on every rank
+             (strong scaling: the total work is fixed).
 """
 import argparse
 import json
@@ -85,37 +90,45 @@ def measured_peaks():
 
 
 def profile_traffic():
-    """DRAM bytes per full D(1e20) from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "k_sweep_traffic.json")
-    if os.path.exists(p):
-        try:
-            return json.load(open(p))
-        except Exception:
-            return None
+    """DRAM bytes per k_sweep launch of D(1e20), from the committed summary
+    of the ncu capture (its line `dram_bytes_per_launch: N`), if present."""
+    p = os.path.join(ROOT, "profiles", "k_sweep_traffic_D1e20.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.strip().startswith("dram_bytes_per_launch:"):
+            try:
+                return {"dram_bytes_per_launch": float(line.split(":", 1)[1].strip().split()[0])}
+            except ValueError:
+                return None
     return None
 
 
 def cpu_baseline(p, threads, target_s=12.0):
-    """Oracle restatement of the reference's chunk loop on a spread sample."""
+    """Oracle restatement of the reference's chunk loop, timed on a sample of
+    D(1e20): nchunks sub-intervals starting at c / nchunks of [0, x/z), all
+    host threads.  The rate is the sample's leaves over its wall time (the
+    metric's unit); the sample fraction grows until it takes about target_s
+    (at most 10x per step while it is tiny, 2x once it takes 0.3 s: its cost
+    grows faster than the fraction, the leaves being densest near 0)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.load()
     nchunks = max(64, 4 * threads)
     frac = 1e-4
     leaves, secs = oracle.D_sample(X, p["y"], p["z"], p["k"], nchunks, frac, threads)
-    # grow the sample until it takes about target_s: at most 10x per step while
-    # the sample is tiny, 3x once it takes 0.3 s (its cost grows faster than
-    # linearly with the fraction)
-    while secs < target_s / 3 and frac < 0.05:
-        step = min(10.0 if secs < 0.3 else 3.0, 0.8 * target_s / max(secs, 1e-3))
+    spent = secs
+    while secs < target_s / 6 and frac < 0.05:
+        step = min(10.0 if secs < 0.3 else 2.0, 0.8 * target_s / max(secs, 1e-3))
         frac = min(0.05, frac * step)
         leaves, secs = oracle.D_sample(X, p["y"], p["z"], p["k"], nchunks, frac, threads)
-    est_total_s = secs / frac
-    return {"value": TOTAL_LEAVES_1E20 / est_total_s, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "oracle chunk loop over %d evenly spread chunks = %.4g of [0, x/z) of D(1e20), "
-                      "%.1f s wall, %d leaves; scaled to the whole interval (est. %.0f s for D(1e20))"
-                      % (nchunks, frac, secs, leaves, est_total_s),
-            "sample_seconds": secs, "est_total_seconds": est_total_s}
+        spent += secs
+    rate = leaves / secs
+    return {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "oracle chunk loop on %d sub-intervals starting at c/%d of [0, x/z) of D(1e20), "
+                      "together %.4g of the interval: %d leaves (%.1f%% of D's) in %.1f s wall on %d threads"
+                      % (nchunks, nchunks, frac, leaves, 100.0 * leaves / TOTAL_LEAVES_1E20, secs, threads),
+            "sample_seconds": secs, "calibration_seconds": spent}
 
 
 def batch_workload(n, seed=20261203):
@@ -242,11 +255,20 @@ def main():
     ctx = pcg.Context(0)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
-    def step():
-        return pcg.D(X, p["y"], p["z"], p["k"], ctx=ctx, stream=sptr)
+    if world > 1:
+        # one D(x) over the N GPUs: this rank sweeps shard `rank` of the
+        # segment plan, then one all-gather of the per-level partials
+        from primecount_gb300.shard import combine_distributed
+
+        def step(c=None, s=None):
+            part = pcg.D_shard(X, p["y"], p["z"], p["k"], rank, world, ctx=c or ctx, stream=s)
+            return combine_distributed(part)
+    else:
+        def step(c=None, s=None):
+            return pcg.D(X, p["y"], p["z"], p["k"], ctx=c or ctx, stream=s)
 
     for _ in range(max(args.warmup, 1)):
-        v = step()
+        v = step(s=sptr)
     stats0 = ctx.last_stats()
 
     rows = []
@@ -266,7 +288,7 @@ def main():
         s_ev = torch.cuda.Event(enable_timing=True)
         e_ev = torch.cuda.Event(enable_timing=True)
         s_ev.record(stream)
-        v = step()
+        v = step(s=sptr)
         e_ev.record(stream)
         evs.append((s_ev, e_ev))
         st = ctx.last_stats()
@@ -284,7 +306,11 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms_step = float(t.item())
     leaves = st["leaves"]
-    value = world * leaves / (ms_step / 1000.0)
+    if dist is not None:
+        t = torch.tensor([leaves], dtype=torch.int64, device="cuda")
+        dist.all_reduce(t)
+        leaves = int(t.item())
+    value = leaves / (ms_step / 1000.0)
 
     # e2e: the C-ABI call on a fresh context (tables built inside the call)
     e2e_t, h2d, d2h = [], 0, 0
@@ -292,7 +318,7 @@ def main():
         c2 = pcg.Context(0)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        v2 = pcg.D(X, p["y"], p["z"], p["k"], ctx=c2)
+        v2 = step(c=c2)
         e2e_t.append(time.perf_counter() - t1)
         s2 = c2.last_stats()
         h2d, d2h = s2["h2d_bytes"], s2["d2h_bytes"]
@@ -303,7 +329,7 @@ def main():
     # pi(x) end to end through the C ABI (pcg_pi, fresh context: every table
     # built inside the call), with the time of each Gourdon term
     pi_line = None
-    if args.pi_steps > 0:
+    if args.pi_steps > 0 and rank == 0:
         ts = []
         for _ in range(args.pi_steps):
             c3 = pcg.Context(0)
@@ -317,9 +343,9 @@ def main():
                    "terms_ms": {"D": s3["d_ms"], "AC": s3["ac_ms"], "B": s3["b_ms"], "Phi0": s3["phi0_ms"],
                                 "Sigma": s3["sigma_ms"], "tables": s3["table_ms"]}}
 
-    batch = run_batch(args, pcg) if args.batch > 0 else None
+    batch = run_batch(args, pcg) if args.batch > 0 and rank == 0 else None
     serve = None
-    if args.serve_seconds > 0:
+    if args.serve_seconds > 0 and rank == 0:
         from primecount_gb300 import serve as sv
         stream = sv.make_stream(20261203, 2000, args.serve_seconds)
         r = sv.run_served(stream, workers=4, max_x=10 ** 20, drain_s=30)
@@ -330,7 +356,10 @@ def main():
     if rank != 0:
         return
     peak, peak_kind = measured_peaks()
-    alg_bytes = 2 * st["factor_entries"] + 4 * st["two_prime_leaves"] + 16 * st["levels"]
+    # 2 B per FactorTableD entry read, 4 B per two-prime leaf (its prime),
+    # 8 B per leaf (the reciprocal of m or of the prime), 16 B per
+    # (segment, level) step (PiTable word of the level bounds)
+    alg_bytes = 2 * st["factor_entries"] + 4 * st["two_prime_leaves"] + 8 * st["leaves"] + 16 * st["levels"]
     k_ms_call = kernel_ms / args.steps
     launches_call = launches / args.steps
     achieved = alg_bytes / (k_ms_call / 1000.0) / 1e9
@@ -344,10 +373,10 @@ def main():
     if not args.no_cpu and X == 10 ** 20:
         cpu = cpu_baseline(p, os.cpu_count() or 1)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "strong",
             "vs_baseline": None, "dtype": "int64/int128", "data": "synthetic (scalar x)",
             "config": {"workload": WORKLOAD if X == 10 ** 20 else "D(%s)" % args.x, "x": args.x, "y": p["y"], "z": p["z"], "k": p["k"],
-                       "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas" if world > 1 else "1 GPU",
+                       "l2": "flushed between steps (256 MiB write)", "parallelism": ("%d shards of the segment plan, one all-gather" % world) if world > 1 else "1 GPU",
                        "segment_words": st["segment_words"], "ctas_per_sm": st["ctas_per_sm"]},
             "result": str(v), "leaves_per_step": leaves,
             "e2e": {"value": leaves / e2e_s, "unit": UNIT, "seconds": e2e_s,

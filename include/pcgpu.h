@@ -116,6 +116,31 @@ pcg_status pcg_D(pcg_i128 x, int64_t y, int64_t z, int64_t k,
 pcg_status pcg_S2_hard(pcg_i128 x, int64_t y, int64_t z, int64_t c,
                        const pcg_opts* opts, pcg_i128* out);
 
+/* One shard of D / S2_hard, for one x swept by several GPUs (one process
+ * per GPU, a contiguous range of the segment plan each).  No counterpart in
+ * the reference, whose chunks of [0, x/z) play the same role inside one
+ * process (src/gourdon/D.cpp:382-421, LoadBalancerS2.cpp).  Shard s of n
+ * sweeps segments [nseg s / n, nseg (s + 1) / n) with the phi offsets counted
+ * from the shard's first number and writes, per level b < cols:
+ *   acc[b]  its leaf sums (the local leaf sums are folded into acc[0]),
+ *   msum[b] the sum of the signed leaf counts -mu of level b,
+ *   csum[b] the numbers of the shard that survive to level b.
+ * *cols = cols (the same for every shard of x).  The arrays hold cap entries;
+ * with cap < cols only *cols is written and PCG_ERANGE is returned.
+ * pcg_shard_combine turns the partials of all shards into the result. */
+pcg_status pcg_D_shard(pcg_i128 x, int64_t y, int64_t z, int64_t k, int shard, int nshards,
+                       const pcg_opts* opts, pcg_i128* acc, int64_t* msum, int64_t* csum,
+                       int64_t cap, int64_t* cols);
+pcg_status pcg_S2_hard_shard(pcg_i128 x, int64_t y, int64_t z, int64_t c, int shard, int nshards,
+                             const pcg_opts* opts, pcg_i128* acc, int64_t* msum, int64_t* csum,
+                             int64_t cap, int64_t* cols);
+
+/* Result of all shards ([nshards][cols] row-major, shards in order):
+ *   sum_s ( sum_b acc_s[b] + msum_s[b] * sum_{s' < s} csum_s'[b] ).
+ * Host arithmetic only (no device work). */
+pcg_status pcg_shard_combine(int nshards, int64_t cols, const pcg_i128* acc, const int64_t* msum,
+                             const int64_t* csum, pcg_i128* out);
+
 /* D(x, y, z, k) without allocating device memory.  No counterpart in the
  * reference.  For callers that cannot call cudaMalloc when they need the
  * result: code running while a stream is being captured into a CUDA graph,

@@ -32,7 +32,8 @@ def build():
 def load():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB):
+        src = os.path.join(HERE, "pcg_oracle.c")
+        if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
             build()
         L = ctypes.CDLL(LIB)
         i64, u64 = ctypes.c_int64, ctypes.c_uint64
@@ -43,6 +44,9 @@ def load():
         L.ora_D_sample.argtypes = [u64, i64, i64, i64, i64, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                    ctypes.POINTER(i64), ctypes.POINTER(ctypes.c_double)]
         L.ora_D_sample.restype = ctypes.c_int
+        L.ora_D_partial.argtypes = [u64, i64, i64, i64, i64, i64, i64, ctypes.POINTER(u64), ctypes.POINTER(i64),
+                                    ctypes.POINTER(i64), ctypes.POINTER(i64), i64]
+        L.ora_D_partial.restype = ctypes.c_int
         L.ora_phi.argtypes = [i64, i64]
         L.ora_phi.restype = i64
         L.ora_pi_sieve.argtypes = [i64]
@@ -85,6 +89,22 @@ def D_sample(x, y, z, k, nchunks, fraction, threads):
     load().ora_D_sample(x & 0xFFFFFFFFFFFFFFFF, x >> 64, y, z, k, nchunks, fraction, threads,
                         ctypes.byref(leaves), ctypes.byref(secs))
     return leaves.value, secs.value
+
+
+def D_partial(x, y, z, k, lo, hi, ncols):
+    """(leaf sum, msum, csum) of the shard [lo, hi) of D with phi offsets
+    counted from lo (the per-shard partials of the multi-GPU split)."""
+    lo_, hi_ = ctypes.c_uint64(), ctypes.c_int64()
+    ms = (ctypes.c_int64 * ncols)()
+    cs = (ctypes.c_int64 * ncols)()
+    rc = load().ora_D_partial(x & 0xFFFFFFFFFFFFFFFF, x >> 64, y, z, k, lo, hi, ctypes.byref(lo_),
+                              ctypes.byref(hi_), ms, cs, ncols)
+    if rc != 0:
+        raise ValueError("oracle rejected the arguments (%d)" % rc)
+    s = (hi_.value << 64) | lo_.value
+    if s >= 1 << 127:
+        s -= 1 << 128
+    return s, list(ms), list(cs)
 
 
 def phi(x, a):

@@ -310,16 +310,69 @@ static void sieve_alloc(osieve* s, int64_t segment_size)
 
 static void sieve_free(osieve* s) { free(s->w); free(s->ctr); }
 
+/* Multiples p q (q coprime to 30) of one prime inside a segment, stepped
+ * along the 30-wheel the way the reference's wheel does (Sieve.cpp:192-216,
+ * lookup_tables.hpp:31-65): the gap to the next co-factor is one of
+ * {6,4,2,4,2,4,6,2}, so the byte (30 numbers) advances by p gap / 30 and the
+ * residue by p gap mod 30, precomputed per prime. */
+static const int WGAP[8] = {6, 4, 2, 4, 2, 4, 6, 2};
+typedef struct {
+  int64_t byte;      /* (p q - low) / 30 */
+  int r;             /* (p q - low) mod 30, coprime to 30 */
+  int j;             /* index of q mod 30 in WOFF */
+  int64_t n;         /* co-factors left */
+  int64_t dbyte[8];
+  int dr[8];
+} wstep;
+
+static int wheel_rank(int64_t q) { return bitpos30[q % 30]; }
+
+/* first co-factor q >= qlo coprime to 30 and the count up to qhi */
+static void wstep_init(wstep* w, int64_t p, int64_t low, int64_t qlo, int64_t qhi)
+{
+  while (qlo <= qhi && wheel_rank(qlo) < 0) qlo++;
+  w->n = 0;
+  if (qlo > qhi) return;
+  /* co-factors coprime to 30 in [qlo, qhi] */
+  int64_t below_hi = 8 * (qhi / 30), below_lo = 8 * ((qlo - 1) / 30);
+  for (int k = 0; k < 8; k++) {
+    if (WOFF[k] <= qhi % 30) below_hi++;
+    if (WOFF[k] <= (qlo - 1) % 30) below_lo++;
+  }
+  w->n = below_hi - below_lo;
+  int64_t off = p * qlo - low;
+  w->byte = off / 30;
+  w->r = (int) (off % 30);
+  w->j = wheel_rank(qlo);
+  for (int k = 0; k < 8; k++) {
+    w->dbyte[k] = p * WGAP[k] / 30;
+    w->dr[k] = (int) (p * WGAP[k] % 30);
+  }
+}
+
+/* the current multiple as (word, bit), then advance */
+static inline void wstep_next(wstep* w, int64_t* wi, uint64_t* bit)
+{
+  *wi = w->byte >> 3;
+  *bit = 1ull << ((w->byte & 7) * 8 + bitpos30[w->r]);
+  int k = w->j;
+  w->r += w->dr[k];
+  w->byte += w->dbyte[k];
+  if (w->r >= 30) { w->r -= 30; w->byte++; }
+  w->j = (k + 1) & 7;
+  w->n--;
+}
+
 static void cross_off_plain(osieve* s, int64_t p)
 {
-  /* n = p * q, q coprime to 30, low <= n < high, n >= p */
-  int64_t qlo = max64((s->low + p - 1) / p, 1);
-  int64_t qhi = (s->high - 1) / p;
-  for (int64_t q = qlo; q <= qhi; q++) {
-    if (bitpos30[q % 30] < 0) continue;
-    int64_t off = p * q - s->low;
-    int64_t wi = off / 240, r = off % 240;
-    s->w[wi] &= ~(1ull << ((r / 30) * 8 + bitpos30[r % 30]));
+  /* n = p * q, q coprime to 30, low <= n < high */
+  wstep w;
+  wstep_init(&w, p, s->low, max64((s->low + p - 1) / p, 1), (s->high - 1) / p);
+  while (w.n > 0) {
+    int64_t wi;
+    uint64_t bit;
+    wstep_next(&w, &wi, &bit);
+    s->w[wi] &= ~bit;
   }
 }
 
@@ -350,7 +403,7 @@ static void sieve_segment_init(osieve* s, int64_t low, int64_t high,
 static void reset_cursor(osieve* s) { s->cur_ctr = 0; s->cur_sum = 0; }
 
 /* number of unsieved numbers in [low, low + stop] (count_stop.hpp:41-89) */
-static uint64_t sieve_count(osieve* s, int64_t stop)
+static inline uint64_t sieve_count(osieve* s, int64_t stop)
 {
   int64_t wi = stop / 240;
   int64_t ci = wi / CTR_WORDS;
@@ -367,14 +420,13 @@ static void sieve_cross_off_count(osieve* s, int64_t p)
 {
   reset_cursor(s);
   if (p < 7) return; /* 2, 3, 5 are not represented in the bitmap */
-  int64_t qlo = max64((s->low + p - 1) / p, 1);
-  int64_t qhi = (s->high - 1) / p;
   uint64_t removed = 0;
-  for (int64_t q = qlo; q <= qhi; q++) {
-    if (bitpos30[q % 30] < 0) continue;
-    int64_t off = p * q - s->low;
-    int64_t wi = off / 240, r = off % 240;
-    uint64_t bit = 1ull << ((r / 30) * 8 + bitpos30[r % 30]);
+  wstep w;
+  wstep_init(&w, p, s->low, max64((s->low + p - 1) / p, 1), (s->high - 1) / p);
+  while (w.n > 0) {
+    int64_t wi;
+    uint64_t bit;
+    wstep_next(&w, &wi, &bit);
     if (s->w[wi] & bit) {
       s->w[wi] &= ~bit;
       s->ctr[wi / CTR_WORDS]--;
@@ -514,8 +566,18 @@ static void chunk_b_bounds(const sweep* w, int64_t low, int64_t limit,
 /* Reference leaf loop over one chunk [low, limit) with phi[b] = phi(low-1, b-1)
  * (D.cpp:106-305; S2_hard.cpp:77-158).  Scalar restatement: the SIMD filter
  * and batching of the reference do not change the set of leaves. */
+static i128 sweep_chunk_m(const sweep* w, int64_t low, int64_t limit, int64_t segment_size,
+                          int64_t* phi, ora_stats* st, int64_t* msum);
+
 static i128 sweep_chunk(const sweep* w, int64_t low, int64_t limit, int64_t segment_size,
                         int64_t* phi, ora_stats* st)
+{
+  return sweep_chunk_m(w, low, limit, segment_size, phi, st, NULL);
+}
+
+/* msum (optional): per level b, the sum of -mu over the chunk's leaves */
+static i128 sweep_chunk_m(const sweep* w, int64_t low, int64_t limit, int64_t segment_size,
+                          int64_t* phi, ora_stats* st, int64_t* msum)
 {
   i128 sum = 0;
   int64_t min_b, max_b;
@@ -558,11 +620,13 @@ static i128 sweep_chunk(const sweep* w, int64_t low, int64_t limit, int64_t segm
         uint32_t f = w->factor[m];
         if ((int64_t) f > threshold) {
           int64_t mnum = to_number((uint64_t) m);
-          int64_t xpm = (int64_t) (xp / (u128) mnum);
+          int64_t xpm = (xp >> 64) == 0 ? (int64_t) ((uint64_t) xp / (uint64_t) mnum)
+                                         : (int64_t) (xp / (u128) mnum);
           int64_t count = (int64_t) sieve_count(&s, xpm - low);
           int64_t phi_xpm = phi[b] + count;
           int64_t mu = (f & 1) ? -1 : 1;
           sum -= (i128) mu * phi_xpm;
+          if (msum) msum[b] -= mu;
           if (st) st->leaves++;
         }
       }
@@ -588,9 +652,11 @@ static i128 sweep_chunk(const sweep* w, int64_t low, int64_t limit, int64_t segm
       }
       if (prime >= w->primes[l]) goto next_segment;
       for (; w->primes[l] > min_hard; l--) {
-        int64_t xpq = (int64_t) (xp / (u128) w->primes[l]);
+        int64_t xpq = (xp >> 64) == 0 ? (int64_t) ((uint64_t) xp / (uint64_t) w->primes[l])
+                                       : (int64_t) (xp / (u128) w->primes[l]);
         int64_t count = (int64_t) sieve_count(&s, xpq - low);
         sum += phi[b] + count;
+        if (msum) msum[b] += 1;
         if (st) { st->leaves++; st->two_prime_leaves++; }
       }
       phi[b] += (int64_t) s.total;
@@ -801,6 +867,62 @@ int ora_D(uint64_t x_lo, int64_t x_hi, int64_t y, int64_t z, int64_t k,
   free(pt.t);
   split128(r, out_lo, out_hi);
   return 0;
+}
+
+/* One shard [lo, hi) of D with phi offsets counted from lo (the
+ * decomposition of pcg_D_shard): the shard's leaf sum *out, per level b the
+ * sum of -mu over its leaves (msum[b]) and the numbers of [lo, hi) that
+ * survive to level b (csum[b], the total_count of D.cpp:271 summed over the
+ * shard's segments).  lo is a multiple of 240.  Single-threaded. */
+int ora_D_partial(uint64_t x_lo, int64_t x_hi, int64_t y, int64_t z, int64_t k, int64_t lo, int64_t hi,
+                  uint64_t* out_lo, int64_t* out_hi, int64_t* msum, int64_t* csum, int64_t ncols)
+{
+  init_tables();
+  u128 x = make_u128(x_lo, x_hi);
+  if (x_hi < 0 || y < 1 || z < 1 || k < 0 || lo < 0 || lo % 240 != 0 || hi < lo) return 1;
+  if (z > 386083ll * 386083 - 1) return 2;
+  sweep w;
+  memset(&w, 0, sizeof(w));
+  w.gourdon = 1;
+  w.x = x;
+  w.y = y;
+  w.z = z;
+  w.k = k;
+  w.limit = (int64_t) (x / (u128) z);
+  w.x_star = x_star_gourdon(x, y);
+  pitable pt;
+  pitable_build(&pt, y);
+  w.pi = &pt;
+  w.pi_sqrt = pit(&pt, (uint64_t) isqrt64(z));
+  int64_t np;
+  int64_t* primes = primes_upto(y, &np);
+  w.primes = primes;
+  w.nprimes = np;
+  int64_t bglob = min64(pit(&pt, (uint64_t) w.x_star), np);
+  int rc = 0;
+  if (ncols < bglob + 1) { rc = 3; goto done; }
+  {
+    int64_t fsz = ora_factor_size(z);
+    uint32_t* factor = (uint32_t*) malloc(sizeof(uint32_t) * (size_t) fsz);
+    factor_build(1, y, z, 0xFFFF, factor);
+    w.factor = factor;
+    for (int64_t b = 0; b < ncols; b++) { msum[b] = 0; csum[b] = 0; }
+    hi = min64(hi, w.limit);
+    i128 r = 0;
+    if (hi > lo) {
+      int64_t seg = pick_segment_size(w.limit);
+      count_chunk(&w, lo, hi, seg, bglob, csum);
+      int64_t* phi = (int64_t*) calloc((size_t) (np + 2), sizeof(int64_t));
+      r = sweep_chunk_m(&w, lo, hi, seg, phi, NULL, msum);
+      free(phi);
+    }
+    free(factor);
+    split128(r, out_lo, out_hi);
+  }
+done:
+  free(primes);
+  free(pt.t);
+  return rc;
 }
 
 int ora_S2_hard(uint64_t x_lo, int64_t x_hi, int64_t y, int64_t z, int64_t c,

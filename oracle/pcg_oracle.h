@@ -41,6 +41,14 @@ typedef struct {
 int ora_D(uint64_t x_lo, int64_t x_hi, int64_t y, int64_t z, int64_t k,
           int threads, uint64_t* out_lo, int64_t* out_hi, ora_stats* stats);
 
+/* One shard [lo, hi) of D with the phi offsets counted from lo (lo a
+ * multiple of 240): the shard's leaf sum, and per level b < ncols the sum of
+ * -mu over its leaves (msum) and its survivors at level b (csum).  The
+ * shards' results combine as sum_s (sum_s + sum_b msum_s[b] * sum_{s'<s}
+ * csum_s'[b]).  Returns 3 when ncols < pi(x_star) + 1. */
+int ora_D_partial(uint64_t x_lo, int64_t x_hi, int64_t y, int64_t z, int64_t k, int64_t lo, int64_t hi,
+                  uint64_t* out_lo, int64_t* out_hi, int64_t* msum, int64_t* csum, int64_t ncols);
+
 /* S2_hard(x, y, z, c), Deleglise-Rivat.
  * Reference: src/deleglise-rivat/S2_hard.cpp:51-161, 181-293. */
 int ora_S2_hard(uint64_t x_lo, int64_t x_hi, int64_t y, int64_t z, int64_t c,

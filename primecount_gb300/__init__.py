@@ -108,9 +108,14 @@ def load(path=None):
     L.primecount_phi.argtypes = [c_i64, c_i64]
     L.primecount_phi.restype = c_i64
     L.primecount_version.restype = ctypes.c_char_p
+    shard_args = [I128, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int, c_p(Opts), c_p(I128), c_p(c_i64),
+                  c_p(c_i64), c_i64, c_p(c_i64)]
+    L.pcg_D_shard.argtypes = shard_args
+    L.pcg_S2_hard_shard.argtypes = shard_args
+    L.pcg_shard_combine.argtypes = [ctypes.c_int, c_i64, c_p(I128), c_p(c_i64), c_p(c_i64), c_p(I128)]
     for name in ("pcg_D", "pcg_S2_hard", "pcg_D_default", "pcg_S2_hard_default", "pcg_gourdon_params",
                  "pcg_dr_params", "pcg_pi", "pcg_phi", "pcg_pi_batch", "pcg_phi_batch", "pcg_ctx_create",
-                 "pcg_last_stats"):
+                 "pcg_last_stats", "pcg_D_shard", "pcg_S2_hard_shard", "pcg_shard_combine"):
         getattr(L, name).restype = ctypes.c_int
     if path is None:
         _lib = L
@@ -258,3 +263,58 @@ def phi_batch(xs, as_, ctx=None, stream=None):
     o = _opts(ctx, stream)
     _check(load().pcg_phi_batch(ax, aa, n, out, ctypes.byref(o)), ctx)
     return list(out)
+
+
+# ---------------------------------------------------------------- shards
+class ShardPart:
+    """Per-level partials of one shard: acc (int), msum, csum (lists of int)."""
+
+    __slots__ = ("acc", "msum", "csum")
+
+    def __init__(self, acc, msum, csum):
+        self.acc, self.msum, self.csum = list(acc), list(msum), list(csum)
+
+
+def _shard(fn, x, y, z, k, shard, nshards, ctx=None, stream=None, cap=1 << 16):
+    cols = ctypes.c_int64()
+    while True:
+        acc = (I128 * cap)()
+        ms = (ctypes.c_int64 * cap)()
+        cs = (ctypes.c_int64 * cap)()
+        o = _opts(ctx, stream)
+        st = fn(to_i128(x), int(y), int(z), int(k), int(shard), int(nshards), ctypes.byref(o), acc, ms, cs,
+                cap, ctypes.byref(cols))
+        if st == 2 and cols.value > cap:
+            cap = cols.value
+            continue
+        _check(st, ctx)
+        n = cols.value
+        return ShardPart([from_i128(acc[i]) for i in range(n)], ms[:n], cs[:n])
+
+
+def D_shard(x, y, z, k, shard, nshards, ctx=None, stream=None):
+    """Shard `shard` of `nshards` of D(x, y, z, k) (pcg_D_shard)."""
+    return _shard(load().pcg_D_shard, x, y, z, k, shard, nshards, ctx, stream)
+
+
+def S2_hard_shard(x, y, z, c, shard, nshards, ctx=None, stream=None):
+    """Shard `shard` of `nshards` of S2_hard(x, y, z, c) (pcg_S2_hard_shard)."""
+    return _shard(load().pcg_S2_hard_shard, x, y, z, c, shard, nshards, ctx, stream)
+
+
+def shard_combine(parts):
+    """The result from the partials of all shards, in shard order
+    (pcg_shard_combine; host arithmetic, no GPU needed)."""
+    n = len(parts)
+    cols = max((len(p.acc) for p in parts), default=0)
+    acc = (I128 * max(1, n * cols))()
+    ms = (ctypes.c_int64 * max(1, n * cols))()
+    cs = (ctypes.c_int64 * max(1, n * cols))()
+    for s_, p in enumerate(parts):
+        for b in range(len(p.acc)):
+            acc[s_ * cols + b] = to_i128(p.acc[b])
+            ms[s_ * cols + b] = p.msum[b]
+            cs[s_ * cols + b] = p.csum[b]
+    out = I128()
+    _check(load().pcg_shard_combine(n, cols, acc, ms, cs, ctypes.byref(out)))
+    return from_i128(out)

@@ -405,6 +405,80 @@ pcg_status pcg_S2_hard(pcg_i128 x, int64_t y, int64_t z, int64_t c, const pcg_op
   return hard_leaves(false, x, y, z, c, opts, out);
 }
 
+// One shard of D / S2_hard (several GPUs, one process each): the shard's
+// per-level partials, combined in shard order by pcg_shard_combine.
+static pcg_status hard_leaves_shard(bool gourdon, pcg_i128 xi, int64_t y, int64_t z, int64_t k, int shard,
+                                    int nshards, const pcg_opts* opts, pcg_i128* acc, int64_t* msum,
+                                    int64_t* csum, int64_t cap, int64_t* cols_out)
+{
+  if (!cols_out) return PCG_EINVAL;
+  Ctx* cp = nullptr;
+  return guard(nullptr, [&] {
+    cp = ctx_from(opts);
+    Ctx& c = *cp;
+    c.last_error.clear();
+    if (xi.hi < 0) fail(PCG_EINVAL, "x must be >= 0");
+    if (nshards < 1 || shard < 0 || shard >= nshards) fail(PCG_EINVAL, "shard must be in [0, nshards)");
+    u128 x = make_u128(xi);
+    *cols_out = 0;
+    if (x < 1) return;
+    check_hard_args(x, y, z, k, gourdon);
+    SweepProblem p;
+    p.gourdon = gourdon ? 1 : 0;
+    p.x = x;
+    p.y = y;
+    p.z = z;
+    p.k = k;
+    p.shard = shard;
+    p.nshards = nshards;
+    p.parts = true;
+    SweepResult r = run_sweep(c, p, tuning_from(opts), stream_from(c, opts));
+    c.last = r.stats;
+    const int64_t cols = (int64_t) r.acc.size();
+    *cols_out = cols;
+    if (cols > cap) fail(PCG_ERANGE, "partial arrays hold " + std::to_string(cap) + " levels, " +
+                                         std::to_string(cols) + " needed");
+    if (cols > 0 && (!acc || !msum || !csum)) fail(PCG_EINVAL, "null partial array");
+    for (int64_t b = 0; b < cols; b++) {
+      acc[b] = to_pcg(r.acc[(size_t) b]);
+      msum[b] = r.msum[(size_t) b];
+      csum[b] = r.csum[(size_t) b];
+    }
+  });
+}
+
+pcg_status pcg_D_shard(pcg_i128 x, int64_t y, int64_t z, int64_t k, int shard, int nshards, const pcg_opts* opts,
+                       pcg_i128* acc, int64_t* msum, int64_t* csum, int64_t cap, int64_t* cols)
+{
+  return hard_leaves_shard(true, x, y, z, k, shard, nshards, opts, acc, msum, csum, cap, cols);
+}
+
+pcg_status pcg_S2_hard_shard(pcg_i128 x, int64_t y, int64_t z, int64_t c, int shard, int nshards,
+                             const pcg_opts* opts, pcg_i128* acc, int64_t* msum, int64_t* csum, int64_t cap,
+                             int64_t* cols)
+{
+  return hard_leaves_shard(false, x, y, z, c, shard, nshards, opts, acc, msum, csum, cap, cols);
+}
+
+pcg_status pcg_shard_combine(int nshards, int64_t cols, const pcg_i128* acc, const int64_t* msum,
+                             const int64_t* csum, pcg_i128* out)
+{
+  if (!out || nshards < 1 || cols < 0) return PCG_EINVAL;
+  return guard(nullptr, [&] {
+    if (cols > 0 && (!acc || !msum || !csum)) fail(PCG_EINVAL, "null partial array");
+    std::vector<i128> offset((size_t) cols, 0);   // survivors before the shard, per level
+    i128 total = 0;
+    for (int s = 0; s < nshards; s++) {
+      const int64_t row = (int64_t) s * cols;
+      for (int64_t b = 0; b < cols; b++) {
+        total += make_i128(acc[row + b]) + (i128) msum[row + b] * offset[(size_t) b];
+        offset[(size_t) b] += csum[row + b];
+      }
+    }
+    *out = to_pcg(total);
+  });
+}
+
 // Allocation-free D for callers that cannot allocate device memory at call
 // time (see include/pcgpu.h): tables from the context, working memory from
 // the library's static device scratch.

@@ -36,6 +36,7 @@ int64_t iroot(u128 x, int n);            // exact floor(x^(1/n)), n in {2,3,4,6}
 inline int64_t isqrt(u128 x) { return iroot(x, 2); }
 inline u128 make_u128(pcg_i128 v) { return ((u128) (uint64_t) v.hi << 64) | v.lo; }
 inline pcg_i128 to_pcg(i128 v) { pcg_i128 r; r.lo = (uint64_t) v; r.hi = (int64_t) (v >> 64); return r; }
+inline i128 make_i128(pcg_i128 v) { return (i128) make_u128(v); }
 std::string to_string(i128 v);
 
 // 2*3*5*7*11 wheel of the FactorTables (reference src/BaseFactorTable.hpp:36-47)
@@ -122,6 +123,10 @@ struct SweepProblem {
   int gourdon;         // 1: D, 0: S2_hard
   u128 x;
   int64_t y, z, k;     // k = c for S2_hard
+  // shard s of n: the contiguous segments [nseg s / n, nseg (s + 1) / n) of
+  // the segment plan; n = 1 sweeps everything
+  int shard = 0, nshards = 1;
+  bool parts = false;  // return the per-level partials of the shard
 };
 
 struct Tuning {
@@ -133,6 +138,13 @@ struct Tuning {
 struct SweepResult {
   i128 sum = 0;
   pcg_stats stats{};
+  // per level b (index 0 unused by levels): the shard's leaf sums with phi
+  // offsets counted from the shard start (acc, the shard's local sums folded
+  // into acc[0]), sum of the signed leaf counts M(s, b) and of the survivor
+  // counts C(s, b) over the shard's segments; [lo, hi) = the shard's numbers
+  std::vector<i128> acc;
+  std::vector<int64_t> msum, csum;
+  int64_t lo = 0, hi = 0;
 };
 
 SweepResult run_sweep(Ctx& c, const SweepProblem& p, const Tuning& t, cudaStream_t s);
@@ -149,7 +161,7 @@ struct Ctx {
   uint64_t mem_budget = 0;
   Tables tab;
   // scratch of the sweep (grown on demand)
-  DevBuf cnt, smu, segsum, run, acc, misc;
+  DevBuf cnt, smu, segsum, run, acc, misc, msum;
   pcg_stats last{};
   std::string last_error;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};

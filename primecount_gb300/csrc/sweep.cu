@@ -878,12 +878,14 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
 
 // ---- phi offsets: acc[b] += sum_s M(s, b) * sum_{s'<s} C(s', b), in segment order
 __global__ void k_combine(const uint32_t* __restrict__ cnt, const int32_t* __restrict__ smu,
-                          int wave_len, int cols, int64_t* __restrict__ run, i128* __restrict__ acc)
+                          int wave_len, int cols, int64_t* __restrict__ run, i128* __restrict__ acc,
+                          int64_t* __restrict__ msum)
 {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= cols) return;
   int64_t r = run[b];
   i128 a = 0;
+  int64_t ms = 0;
   int s = 0;
   for (; s + 4 <= wave_len; s += 4) {
     int32_t m0 = smu[(int64_t) s * cols + b], m1 = smu[(int64_t) (s + 1) * cols + b];
@@ -894,13 +896,17 @@ __global__ void k_combine(const uint32_t* __restrict__ cnt, const int32_t* __res
     a += (i128) m1 * r; r += c1;
     a += (i128) m2 * r; r += c2;
     a += (i128) m3 * r; r += c3;
+    ms += (int64_t) m0 + m1 + m2 + m3;
   }
   for (; s < wave_len; s++) {
-    a += (i128) smu[(int64_t) s * cols + b] * r;
+    const int32_t m = smu[(int64_t) s * cols + b];
+    a += (i128) m * r;
+    ms += m;
     r += cnt[(int64_t) s * cols + b];
   }
   run[b] = r;
   acc[b] += a;
+  if (msum) msum[b] += ms;
 }
 
 // ---- local leaf sums of a wave into acc[0] (column 0 is never a level)
@@ -1383,16 +1389,25 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   segbuf.alloc(seglo.size() * 8);
   PCG_CUDA(cudaMemcpyAsync(segbuf.p, seglo.data(), seglo.size() * 8, cudaMemcpyHostToDevice, s));
 
+  // this call's segments: shard pb.shard of pb.nshards (all of them by default)
+  if (pb.nshards < 1 || pb.shard < 0 || pb.shard >= pb.nshards) fail(PCG_EINVAL, "invalid shard");
+  const int64_t seg_begin = nseg * pb.shard / pb.nshards;
+  const int64_t seg_end = nseg * (pb.shard + 1) / pb.nshards;
+  const int64_t nmine = seg_end - seg_begin;
+  res.lo = seglo[(size_t) seg_begin];
+  res.hi = seglo[(size_t) seg_end];
+
   int64_t wave_cap = (int64_t) grid * 8;
   // budget of the C/M matrices: 1 GiB
   int64_t max_rows = std::max<int64_t>(1, (int64_t) (1ull << 30) / ((int64_t) cols * 8));
-  int64_t wave_len = std::min<int64_t>({nseg, wave_cap, max_rows});
+  int64_t wave_len = std::max<int64_t>(1, std::min<int64_t>({nmine, wave_cap, max_rows}));
 
   c.cnt.alloc((size_t) wave_len * cols * 4);
   c.smu.alloc((size_t) wave_len * cols * 4);
   c.segsum.alloc((size_t) wave_len * 8);
   c.run.alloc((size_t) cols * 8);
   c.acc.alloc((size_t) cols * 16);
+  c.msum.alloc((size_t) cols * 8);
   c.misc.alloc(4096);
   uint64_t* d_xp = nullptr;
   DevBuf xpbuf;
@@ -1401,6 +1416,7 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   PCG_CUDA(cudaMemcpyAsync(d_xp, xp.data(), xp.size() * 8, cudaMemcpyHostToDevice, s));
   PCG_CUDA(cudaMemsetAsync(c.run.p, 0, (size_t) cols * 8, s));
   PCG_CUDA(cudaMemsetAsync(c.acc.p, 0, (size_t) cols * 16, s));
+  PCG_CUDA(cudaMemsetAsync(c.msum.p, 0, (size_t) cols * 8, s));
   PCG_CUDA(cudaMemsetAsync(c.misc.p, 0, 4096, s));
   unsigned long long* d_counters = (unsigned long long*) c.misc.p;
   int* d_queue = (int*) ((char*) c.misc.p + 256);   // after the 32 counters
@@ -1439,8 +1455,8 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   uint64_t launches = 0;
   float ms_sweep = 0;
   int waves = 0;
-  for (int64_t first = 0; first < nseg; first += wave_len) {
-    int wl = (int) std::min<int64_t>(wave_len, nseg - first);
+  for (int64_t first = seg_begin; first < seg_end; first += wave_len) {
+    int wl = (int) std::min<int64_t>(wave_len, seg_end - first);
     a.wave_first = first;
     a.wave_len = wl;
     a.queue = d_queue + (waves % 16);
@@ -1459,7 +1475,8 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
     else { if (fbytes == 2) launch_sweep<uint16_t, 128>(a, g, smem, s); else launch_sweep<uint32_t, 128>(a, g, smem, s); }
     PCG_CUDA(cudaGetLastError());
     PCG_CUDA(cudaEventRecord(c.kev[2 * waves + 1], s));
-    k_combine<<<(cols + 255) / 256, 256, 0, s>>>(a.cnt, a.smu, wl, cols, c.run.as<int64_t>(), c.acc.as<i128>());
+    k_combine<<<(cols + 255) / 256, 256, 0, s>>>(a.cnt, a.smu, wl, cols, c.run.as<int64_t>(), c.acc.as<i128>(),
+                                                 c.msum.as<int64_t>());
     k_segsum<<<1, 1024, 0, s>>>(a.segsum, wl, c.acc.as<i128>());
     PCG_CUDA(cudaGetLastError());
     launches += 3;
@@ -1470,7 +1487,14 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   unsigned long long ctr[4];
   PCG_CUDA(cudaMemcpyAsync(acc.data(), c.acc.p, (size_t) cols * 16, cudaMemcpyDeviceToHost, s));
   PCG_CUDA(cudaMemcpyAsync(ctr, d_counters, sizeof(ctr), cudaMemcpyDeviceToHost, s));
+  if (pb.parts) {
+    res.msum.resize((size_t) cols);
+    res.csum.resize((size_t) cols);
+    PCG_CUDA(cudaMemcpyAsync(res.msum.data(), c.msum.p, (size_t) cols * 8, cudaMemcpyDeviceToHost, s));
+    PCG_CUDA(cudaMemcpyAsync(res.csum.data(), c.run.p, (size_t) cols * 8, cudaMemcpyDeviceToHost, s));
+  }
   PCG_CUDA(cudaStreamSynchronize(s));
+  if (pb.parts) res.acc = acc;
   PCG_CUDA(cudaEventElapsedTime(&ms_sweep, c.ev[0], c.ev[1]));
   double kms = 0;
   for (int w = 0; w < waves; w++) {
@@ -1489,7 +1513,7 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   st.two_prime_leaves = ctr[1];
   st.levels = ctr[2];
   st.factor_entries = ctr[3];
-  st.segments = (uint64_t) nseg;
+  st.segments = (uint64_t) nmine;
   st.kernel_launches = launches;
   st.sweep_ms = ms_sweep;
   st.combine_ms = ms_sweep - kms;
@@ -1754,7 +1778,7 @@ SweepResult run_sweep_noalloc(Ctx& c, const SweepProblem& pb, cudaStream_t s)
     if (fbytes == 2) launch_sweep<uint16_t, 256>(a, g, smem, s);
     else launch_sweep<uint32_t, 256>(a, g, smem, s);
     PCG_CUDA(cudaGetLastError());
-    k_combine<<<(cols + 255) / 256, 256, 0, s>>>(d_cnt, d_smu, wl, cols, d_run, d_acc);
+    k_combine<<<(cols + 255) / 256, 256, 0, s>>>(d_cnt, d_smu, wl, cols, d_run, d_acc, nullptr);
     k_segsum<<<1, 1024, 0, s>>>(d_segsum, wl, d_acc);
     PCG_CUDA(cudaGetLastError());
     launches += 3;
