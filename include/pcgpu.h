@@ -68,6 +68,8 @@ typedef struct {
   int segment_words;     /* sieve segment in 64-bit words (x240 numbers); 0 = autotune */
   int ctas_per_sm;       /* resident CTAs per SM for the sweep; 0 = autotune           */
   int cta_threads;       /* threads per sweep CTA: 128, 256 or 512; 0 = autotune       */
+  double alpha_y;        /* pi(x) by Gourdon: y = alpha_y x^(1/3) (the reference's      */
+  double alpha_z;        /* --alpha-y / --alpha-z, z = alpha_z y); <= 0 = default       */
 } pcg_opts;
 
 /* Work and time of the last call on a context. */

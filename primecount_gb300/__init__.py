@@ -40,7 +40,7 @@ class I128(ctypes.Structure):
 class Opts(ctypes.Structure):
     _fields_ = [("ctx", ctypes.c_void_p), ("stream", ctypes.c_void_p), ("threads", ctypes.c_int),
                 ("print", ctypes.c_int), ("segment_words", ctypes.c_int), ("ctas_per_sm", ctypes.c_int),
-                ("cta_threads", ctypes.c_int)]
+                ("cta_threads", ctypes.c_int), ("alpha_y", ctypes.c_double), ("alpha_z", ctypes.c_double)]
 
 
 class Stats(ctypes.Structure):
@@ -160,8 +160,11 @@ class Context:
         return s.as_dict()
 
 
-def _opts(ctx=None, stream=None, threads=0, print_=False, segment_words=0, ctas_per_sm=0, cta_threads=0):
+def _opts(ctx=None, stream=None, threads=0, print_=False, segment_words=0, ctas_per_sm=0, cta_threads=0,
+          alpha_y=0.0, alpha_z=0.0):
     o = Opts()
+    o.alpha_y = alpha_y
+    o.alpha_z = alpha_z
     o.ctx = ctx._h if ctx is not None else None
     o.stream = stream
     o.threads = threads
@@ -220,19 +223,20 @@ def S2_hard_default(x, **kw):
     return S2_hard(x, p["y"], p["z"], p["c"], **kw)
 
 
-def pi(x, threads=0, print=False, ctx=None, stream=None):
-    """Number of primes <= x (primecount::pi)."""
+def pi(x, threads=0, print=False, ctx=None, stream=None, alpha_y=0.0, alpha_z=0.0):
+    """Number of primes <= x (primecount::pi); alpha_y / alpha_z tune
+    Gourdon's y and z (the reference's --alpha-y / --alpha-z)."""
     out = I128()
-    o = _opts(ctx, stream, threads, print)
+    o = _opts(ctx, stream, threads, print, alpha_y=alpha_y, alpha_z=alpha_z)
     _check(load().pcg_pi(to_i128(x), ctypes.byref(o), ctypes.byref(out)), ctx)
     return from_i128(out)
 
 
-def pi_terms(x, ctx=None, stream=None):
+def pi_terms(x, ctx=None, stream=None, alpha_y=0.0, alpha_z=0.0):
     """The terms of Gourdon's formula for x > 1e10 (the reference's --AC, --B,
     --D, --Phi0, --Sigma options): dict with AC, B, D, Phi0, Sigma and pi."""
     out = (I128 * 6)()
-    o = _opts(ctx, stream)
+    o = _opts(ctx, stream, alpha_y=alpha_y, alpha_z=alpha_z)
     _check(load().pcg_pi_terms(to_i128(x), ctypes.byref(o), out), ctx)
     v = [from_i128(t) for t in out]
     return dict(zip(("AC", "B", "D", "Phi0", "Sigma", "pi"), v))

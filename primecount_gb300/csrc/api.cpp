@@ -106,7 +106,9 @@ int64_t x_star_gourdon(u128 x, int64_t y)
   return std::max<int64_t>(xs, 1);
 }
 
-GourdonParams gourdon_params(u128 x)
+GourdonParams gourdon_params(u128 x) { return gourdon_params(x, 0, 0); }
+
+GourdonParams gourdon_params(u128 x, double user_alpha_y, double user_alpha_z)
 {
   double x16 = (double) iroot(x, 6);
   double logx = std::log((double) x);
@@ -120,6 +122,8 @@ GourdonParams gourdon_params(u128 x)
   }
   double alpha_z = in_between(1, alpha_yz / 5, 1.0);
   double alpha_y = alpha_yz / alpha_z;
+  if (user_alpha_y > 0) alpha_y = user_alpha_y;
+  if (user_alpha_z > 0) alpha_z = user_alpha_z;
   alpha_y = in_between(1, alpha_y, x16);
   alpha_y = truncate3(alpha_y);
   alpha_z = truncate3(alpha_z);
@@ -264,6 +268,8 @@ static Tuning tuning_from(const pcg_opts* o)
     t.segment_words = o->segment_words;
     t.ctas_per_sm = o->ctas_per_sm;
     t.cta_threads = o->cta_threads;
+    t.alpha_y = o->alpha_y;
+    t.alpha_z = o->alpha_z;
   }
   return t;
 }

@@ -775,7 +775,7 @@ static void ensure_pibig(Ctx& c, int64_t limit, cudaStream_t s)
 static PiParts pi_gourdon(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s)
 {
   PiParts R;
-  GourdonParams g = gourdon_params(x);
+  GourdonParams g = gourdon_params(x, tune.alpha_y, tune.alpha_z);
   const int64_t y = g.y, z = g.z, k = g.k, x_star = g.x_star;
   if (x > ((u128) y << 62)) fail(PCG_ERANGE, "pi_gourdon(x): x is too large");
   const int64_t sqrtx = isqrt(x);

@@ -53,6 +53,9 @@ const Wheel2310& wheel2310();
 struct GourdonParams { int64_t y, z, k, x_star; };
 struct DrParams { int64_t y, z, c; };
 GourdonParams gourdon_params(u128 x);    // src/gourdon/pi_gourdon.cpp:44-62
+// the same with alpha_y / alpha_z given (<= 0: default), clamped as the
+// reference clamps --alpha-y / --alpha-z (src/gourdon/pi_gourdon.cpp:44-62)
+GourdonParams gourdon_params(u128 x, double alpha_y, double alpha_z);
 DrParams dr_params(u128 x);              // src/app/main.cpp:435-461
 int64_t x_star_gourdon(u128 x, int64_t y);   // src/util.cpp:362-386
 int64_t get_c(int64_t y);                // src/PhiTiny.hpp:47-50
@@ -133,6 +136,7 @@ struct Tuning {
   int segment_words = 0;
   int ctas_per_sm = 0;
   int cta_threads = 0;
+  double alpha_y = 0, alpha_z = 0;   // pi(x) by Gourdon; <= 0: the reference's defaults
 };
 
 struct SweepResult {

@@ -27,6 +27,8 @@ Tuning tune_of(const pcg_opts* o)
     t.segment_words = o->segment_words;
     t.ctas_per_sm = o->ctas_per_sm;
     t.cta_threads = o->cta_threads;
+    t.alpha_y = o->alpha_y;
+    t.alpha_z = o->alpha_z;
   }
   return t;
 }
