@@ -70,6 +70,16 @@ typedef struct {
   int cta_threads;       /* threads per sweep CTA: 128, 256 or 512; 0 = autotune       */
   double alpha_y;        /* pi(x) by Gourdon: y = alpha_y x^(1/3) (the reference's      */
   double alpha_z;        /* --alpha-y / --alpha-z, z = alpha_z y); <= 0 = default       */
+  /* Checkpoint / resume of D and S2_hard (no counterpart in the reference).
+   * With a file path, a sweep resumes from the file when it holds a
+   * checkpoint of the same problem and segment plan, writes the file after a
+   * wave once checkpoint_interval seconds have passed since the last write
+   * (0: after every wave), and removes it when the result is complete.
+   * stop_after_waves > 0 ends the call after that many waves of this call
+   * with PCG_ECANCELLED and the checkpoint written (an orderly interruption). */
+  const char* checkpoint;
+  double checkpoint_interval;
+  int stop_after_waves;
 } pcg_opts;
 
 /* Work and time of the last call on a context. */

@@ -40,7 +40,9 @@ class I128(ctypes.Structure):
 class Opts(ctypes.Structure):
     _fields_ = [("ctx", ctypes.c_void_p), ("stream", ctypes.c_void_p), ("threads", ctypes.c_int),
                 ("print", ctypes.c_int), ("segment_words", ctypes.c_int), ("ctas_per_sm", ctypes.c_int),
-                ("cta_threads", ctypes.c_int), ("alpha_y", ctypes.c_double), ("alpha_z", ctypes.c_double)]
+                ("cta_threads", ctypes.c_int), ("alpha_y", ctypes.c_double), ("alpha_z", ctypes.c_double),
+                ("checkpoint", ctypes.c_char_p), ("checkpoint_interval", ctypes.c_double),
+                ("stop_after_waves", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -161,10 +163,13 @@ class Context:
 
 
 def _opts(ctx=None, stream=None, threads=0, print_=False, segment_words=0, ctas_per_sm=0, cta_threads=0,
-          alpha_y=0.0, alpha_z=0.0):
+          alpha_y=0.0, alpha_z=0.0, checkpoint=None, checkpoint_interval=0.0, stop_after_waves=0):
     o = Opts()
     o.alpha_y = alpha_y
     o.alpha_z = alpha_z
+    o.checkpoint = os.fsencode(checkpoint) if checkpoint else None
+    o.checkpoint_interval = checkpoint_interval
+    o.stop_after_waves = stop_after_waves
     o.ctx = ctx._h if ctx is not None else None
     o.stream = stream
     o.threads = threads
@@ -181,19 +186,23 @@ def last_stats(ctx=None):
     return s.as_dict()
 
 
-def D(x, y, z, k, threads=0, print=False, ctx=None, stream=None, segment_words=0, ctas_per_sm=0, cta_threads=0):
-    """Gourdon's D(x, y, z, k): the hard special leaves (src/gourdon/D.cpp)."""
+def D(x, y, z, k, threads=0, print=False, ctx=None, stream=None, segment_words=0, ctas_per_sm=0, cta_threads=0,
+      checkpoint=None, checkpoint_interval=0.0, stop_after_waves=0):
+    """Gourdon's D(x, y, z, k): the hard special leaves (src/gourdon/D.cpp).
+    checkpoint: file to resume from / save to (see pcg_opts in pcgpu.h)."""
     out = I128()
-    o = _opts(ctx, stream, threads, print, segment_words, ctas_per_sm, cta_threads)
+    o = _opts(ctx, stream, threads, print, segment_words, ctas_per_sm, cta_threads,
+              checkpoint=checkpoint, checkpoint_interval=checkpoint_interval, stop_after_waves=stop_after_waves)
     _check(load().pcg_D(to_i128(x), int(y), int(z), int(k), ctypes.byref(o), ctypes.byref(out)), ctx)
     return from_i128(out)
 
 
 def S2_hard(x, y, z, c, threads=0, print=False, ctx=None, stream=None, segment_words=0, ctas_per_sm=0,
-            cta_threads=0):
+            cta_threads=0, checkpoint=None, checkpoint_interval=0.0, stop_after_waves=0):
     """Deleglise-Rivat's S2_hard(x, y, z, c) (src/deleglise-rivat/S2_hard.cpp)."""
     out = I128()
-    o = _opts(ctx, stream, threads, print, segment_words, ctas_per_sm, cta_threads)
+    o = _opts(ctx, stream, threads, print, segment_words, ctas_per_sm, cta_threads,
+              checkpoint=checkpoint, checkpoint_interval=checkpoint_interval, stop_after_waves=stop_after_waves)
     _check(load().pcg_S2_hard(to_i128(x), int(y), int(z), int(c), ctypes.byref(o), ctypes.byref(out)), ctx)
     return from_i128(out)
 

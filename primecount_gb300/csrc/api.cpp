@@ -270,6 +270,9 @@ static Tuning tuning_from(const pcg_opts* o)
     t.cta_threads = o->cta_threads;
     t.alpha_y = o->alpha_y;
     t.alpha_z = o->alpha_z;
+    if (o->checkpoint) t.checkpoint = o->checkpoint;
+    t.checkpoint_interval = o->checkpoint_interval;
+    t.stop_after_waves = o->stop_after_waves;
   }
   return t;
 }

@@ -137,6 +137,9 @@ struct Tuning {
   int ctas_per_sm = 0;
   int cta_threads = 0;
   double alpha_y = 0, alpha_z = 0;   // pi(x) by Gourdon; <= 0: the reference's defaults
+  std::string checkpoint;            // sweep checkpoint file ("" = none)
+  double checkpoint_interval = 0;    // seconds between checkpoint writes
+  int stop_after_waves = 0;          // > 0: stop (checkpointed) after this many waves
 };
 
 struct SweepResult {

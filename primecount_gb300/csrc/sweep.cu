@@ -1305,6 +1305,71 @@ static std::vector<int64_t> plan_segments(const SweepProblem& pb, const Tables& 
   return seg;
 }
 
+// ---- checkpoint / resume of a sweep: the phi-offset totals run[b], the leaf
+// sums acc[b] and msum[b] after the last finished wave, with the problem and
+// a hash of the segment plan they belong to
+struct CkptHeader {
+  char magic[8];
+  uint32_t version;
+  int32_t gourdon;
+  uint64_t x_lo, x_hi;
+  int64_t y, z, k;
+  int32_t shard, nshards;
+  int32_t words, nt;
+  int64_t nseg, cols;
+  uint64_t plan_hash;
+  int64_t next_first;      // first segment not swept yet
+  int64_t waves;
+  uint64_t counters[4];
+};
+
+static uint64_t plan_hash(const std::vector<int64_t>& seglo)
+{
+  uint64_t h = 1469598103934665603ull;   // FNV-1a over the segment bounds
+  for (int64_t v : seglo)
+    for (int i = 0; i < 8; i++) { h ^= (uint64_t) (v >> (8 * i)) & 0xFF; h *= 1099511628211ull; }
+  return h;
+}
+
+static bool same_problem(const CkptHeader& a, const CkptHeader& b)
+{
+  return memcmp(a.magic, b.magic, 8) == 0 && a.version == b.version && a.gourdon == b.gourdon &&
+         a.x_lo == b.x_lo && a.x_hi == b.x_hi && a.y == b.y && a.z == b.z && a.k == b.k && a.shard == b.shard &&
+         a.nshards == b.nshards && a.words == b.words && a.nt == b.nt && a.nseg == b.nseg && a.cols == b.cols &&
+         a.plan_hash == b.plan_hash;
+}
+
+static bool read_checkpoint(const std::string& path, const CkptHeader& want, CkptHeader& got,
+                            std::vector<int64_t>& run, std::vector<i128>& acc, std::vector<int64_t>& msum)
+{
+  FILE* f = fopen(path.c_str(), "rb");
+  if (!f) return false;
+  bool ok = fread(&got, sizeof(got), 1, f) == 1 && same_problem(got, want) && got.next_first >= 0 &&
+            got.next_first <= got.nseg;
+  const size_t n = (size_t) want.cols;
+  if (ok) {
+    run.resize(n);
+    acc.resize(n);
+    msum.resize(n);
+    ok = fread(run.data(), 8, n, f) == n && fread(acc.data(), 16, n, f) == n && fread(msum.data(), 8, n, f) == n;
+  }
+  fclose(f);
+  return ok;
+}
+
+static void write_checkpoint(const std::string& path, const CkptHeader& h, const std::vector<int64_t>& run,
+                             const std::vector<i128>& acc, const std::vector<int64_t>& msum)
+{
+  const std::string tmp = path + ".tmp";
+  FILE* f = fopen(tmp.c_str(), "wb");
+  if (!f) fail(PCG_EINVAL, "cannot write the checkpoint " + tmp);
+  const size_t n = run.size();
+  bool ok = fwrite(&h, sizeof(h), 1, f) == 1 && fwrite(run.data(), 8, n, f) == n &&
+            fwrite(acc.data(), 16, n, f) == n && fwrite(msum.data(), 8, n, f) == n;
+  ok = (fclose(f) == 0) && ok;
+  if (!ok || rename(tmp.c_str(), path.c_str()) != 0) fail(PCG_EINVAL, "cannot write the checkpoint " + path);
+}
+
 SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaStream_t s)
 {
   SweepResult res;
@@ -1451,11 +1516,60 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   a.segsum = c.segsum.as<int64_t>();
   a.counters = d_counters;
 
+  // resume from a checkpoint of the same problem and plan
+  CkptHeader ck;
+  memset(&ck, 0, sizeof(ck));
+  memcpy(ck.magic, "PCGSWEEP", 8);
+  ck.version = 1;
+  ck.gourdon = pb.gourdon;
+  ck.x_lo = (uint64_t) x;
+  ck.x_hi = (uint64_t) (x >> 64);
+  ck.y = pb.y;
+  ck.z = pb.z;
+  ck.k = pb.k;
+  ck.shard = pb.shard;
+  ck.nshards = pb.nshards;
+  ck.words = words;
+  ck.nt = NT;
+  ck.nseg = nseg;
+  ck.cols = cols;
+  ck.plan_hash = plan_hash(seglo);
+  const bool use_ckpt = !tune.checkpoint.empty();
+  int64_t start_first = seg_begin;
+  if (use_ckpt) {
+    CkptHeader got;
+    std::vector<int64_t> r0, m0;
+    std::vector<i128> a0;
+    if (read_checkpoint(tune.checkpoint, ck, got, r0, a0, m0) && got.next_first >= seg_begin &&
+        got.next_first <= seg_end) {
+      PCG_CUDA(cudaMemcpyAsync(c.run.p, r0.data(), (size_t) cols * 8, cudaMemcpyHostToDevice, s));
+      PCG_CUDA(cudaMemcpyAsync(c.acc.p, a0.data(), (size_t) cols * 16, cudaMemcpyHostToDevice, s));
+      PCG_CUDA(cudaMemcpyAsync(c.msum.p, m0.data(), (size_t) cols * 8, cudaMemcpyHostToDevice, s));
+      PCG_CUDA(cudaMemcpyAsync(d_counters, got.counters, sizeof(got.counters), cudaMemcpyHostToDevice, s));
+      PCG_CUDA(cudaStreamSynchronize(s));
+      start_first = got.next_first;
+      ck.waves = got.waves;
+    }
+  }
+  double last_write = now_ms();
+  auto save = [&](int64_t next_first) {
+    std::vector<int64_t> r0((size_t) cols), m0((size_t) cols);
+    std::vector<i128> a0((size_t) cols);
+    PCG_CUDA(cudaMemcpyAsync(r0.data(), c.run.p, (size_t) cols * 8, cudaMemcpyDeviceToHost, s));
+    PCG_CUDA(cudaMemcpyAsync(a0.data(), c.acc.p, (size_t) cols * 16, cudaMemcpyDeviceToHost, s));
+    PCG_CUDA(cudaMemcpyAsync(m0.data(), c.msum.p, (size_t) cols * 8, cudaMemcpyDeviceToHost, s));
+    PCG_CUDA(cudaMemcpyAsync(ck.counters, d_counters, sizeof(ck.counters), cudaMemcpyDeviceToHost, s));
+    PCG_CUDA(cudaStreamSynchronize(s));
+    ck.next_first = next_first;
+    write_checkpoint(tune.checkpoint, ck, r0, a0, m0);
+    last_write = now_ms();
+  };
+
   PCG_CUDA(cudaEventRecord(c.ev[0], s));
   uint64_t launches = 0;
   float ms_sweep = 0;
   int waves = 0;
-  for (int64_t first = seg_begin; first < seg_end; first += wave_len) {
+  for (int64_t first = start_first; first < seg_end; first += wave_len) {
     int wl = (int) std::min<int64_t>(wave_len, seg_end - first);
     a.wave_first = first;
     a.wave_len = wl;
@@ -1481,6 +1595,15 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
     PCG_CUDA(cudaGetLastError());
     launches += 3;
     waves++;
+    ck.waves++;
+    const int64_t next = std::min<int64_t>(first + wave_len, seg_end);
+    if (use_ckpt && next < seg_end) {
+      const bool stop = tune.stop_after_waves > 0 && waves >= tune.stop_after_waves;
+      if (stop || now_ms() - last_write >= 1000.0 * tune.checkpoint_interval) save(next);
+      if (stop)
+        fail(PCG_ECANCELLED, "sweep stopped after " + std::to_string(waves) + " waves; checkpoint written to " +
+                                 tune.checkpoint);
+    }
   }
   PCG_CUDA(cudaEventRecord(c.ev[1], s));
   std::vector<i128> acc((size_t) cols);
@@ -1515,6 +1638,7 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   st.factor_entries = ctr[3];
   st.segments = (uint64_t) nmine;
   st.kernel_launches = launches;
+  if (use_ckpt) remove(tune.checkpoint.c_str());
   st.sweep_ms = ms_sweep;
   st.combine_ms = ms_sweep - kms;
   st.segment_words = words;
