@@ -189,23 +189,63 @@ static __device__ __forceinline__ long long pi_pt(const ulonglong2* __restrict__
 }
 
 template <int MODE>
+__device__ __forceinline__ long long pair_term(const PairOuter& O, int64_t i, uint32_t q, uint64_t m,
+                                              const ulonglong2* __restrict__ pt, const uint64_t* s_mask)
+{
+  uint64_t n;
+  if (O.xp_hi == 0) n = div_magic(O.xp_lo, q, m);
+  else n = (uint64_t) ((((u128) O.xp_hi << 64) | O.xp_lo) / q);
+  const long long pin = n < 6 ? (long long) ((0x322100u >> (4 * n)) & 15u) : pi_pt(pt, s_mask, n);
+  if (MODE == 0) return (q <= O.cap) ? pin : 2 * pin;
+  if (MODE == 1) return pin - O.b + 2;
+  if (MODE == 2) return -(pin - O.b + 2);
+  return pin - i + 1;
+}
+
+// the terms of one outer, 256 threads, four terms per thread in flight
+template <int MODE>
 __device__ __forceinline__ long long pair_terms(const PairOuter& O, const uint32_t* __restrict__ primes,
                                                 const uint64_t* __restrict__ magic,
                                                 const ulonglong2* __restrict__ pt, const uint64_t* s_mask)
 {
   long long s = 0;
-  for (int64_t i = O.i_lo + 1 + threadIdx.x; i <= O.i_hi; i += blockDim.x) {
-    const uint32_t q = primes[i];
-    uint64_t n;
-    if (O.xp_hi == 0) n = div_magic(O.xp_lo, q, magic[i]);
-    else n = (uint64_t) ((((u128) O.xp_hi << 64) | O.xp_lo) / q);
-    const long long pin = n < 6 ? (long long) ((0x322100u >> (4 * n)) & 15u) : pi_pt(pt, s_mask, n);
-    if (MODE == 0) s += (q <= O.cap) ? pin : 2 * pin;
-    else if (MODE == 1) s += pin - O.b + 2;
-    else if (MODE == 2) s -= pin - O.b + 2;
-    else s += pin - i + 1;
+  int64_t i = O.i_lo + 1 + threadIdx.x;
+  for (; i + 3 * 256 <= O.i_hi; i += 4 * 256) {
+    uint32_t q[4];
+    uint64_t m[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) { q[u] = primes[i + 256 * u]; m[u] = magic[i + 256 * u]; }
+#pragma unroll
+    for (int u = 0; u < 4; u++) s += pair_term<MODE>(O, i + 256 * u, q[u], m[u], pt, s_mask);
   }
+  for (; i <= O.i_hi; i += 256) s += pair_term<MODE>(O, i, primes[i], magic[i], pt, s_mask);
   return s;
+}
+
+// outers of more than PAIR_SPLIT terms are cut into pieces of PAIR_SPLIT so
+// that the pieces spread evenly over the blocks
+#define PAIR_SPLIT 16384
+__global__ void k_pair_pieces(const PairOuter* __restrict__ outs, int64_t n, uint32_t* __restrict__ pieces)
+{
+  const int64_t j = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (j > n) return;
+  const int64_t c = j < n ? dmax(0, outs[j].i_hi - outs[j].i_lo) : 0;
+  pieces[j] = (uint32_t) ((c + PAIR_SPLIT - 1) / PAIR_SPLIT);
+}
+
+__global__ void k_pair_split(const PairOuter* __restrict__ outs, int64_t n, const uint64_t* __restrict__ first,
+                             PairOuter* __restrict__ split)
+{
+  const int64_t j = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const PairOuter O = outs[j];
+  const int64_t np = (int64_t) (first[j + 1] - first[j]);
+  for (int64_t t = 0; t < np; t++) {
+    PairOuter P = O;
+    P.i_lo = O.i_lo + t * PAIR_SPLIT;
+    P.i_hi = dmin(O.i_hi, P.i_lo + PAIR_SPLIT);
+    split[first[j] + t] = P;
+  }
 }
 
 __global__ void __launch_bounds__(256) k_pairs(const PairOuter* __restrict__ outs, int64_t n_outer,
@@ -228,6 +268,37 @@ __global__ void __launch_bounds__(256) k_pairs(const PairOuter* __restrict__ out
     acc += s;
   }
   block_sum_i128<256>(acc, &partial[blockIdx.x]);
+}
+
+// sum of the terms of nout outers: big outers cut into pieces, then one
+// block per piece
+static i128 run_pairs(Ctx& c, const PairOuter* outs, int64_t nout, cudaStream_t s, uint64_t* launches)
+{
+  if (nout <= 0) return 0;
+  DevBuf pieces, first;
+  pieces.alloc((size_t) (nout + 1) * 4);
+  first.alloc((size_t) (nout + 1) * 8);
+  k_pair_pieces<<<(unsigned) ((nout + 256) / 256), 256, 0, s>>>(outs, nout, pieces.as<uint32_t>());
+  PCG_CUDA(cudaGetLastError());
+  exclusive_scan_u32(pieces.as<uint32_t>(), nout + 1, first.as<uint64_t>(), s);
+  uint64_t np = 0;
+  PCG_CUDA(cudaMemcpyAsync(&np, first.as<uint64_t>() + nout, 8, cudaMemcpyDeviceToHost, s));
+  PCG_CUDA(cudaStreamSynchronize(s));
+  if (np == 0) return 0;
+  DevBuf split;
+  split.alloc((size_t) np * sizeof(PairOuter));
+  k_pair_split<<<(unsigned) ((nout + 127) / 128), 128, 0, s>>>(outs, nout, first.as<uint64_t>(),
+                                                               split.as<PairOuter>());
+  PCG_CUDA(cudaGetLastError());
+  const int grid = (int) std::min<uint64_t>(np, (uint64_t) c.num_sms * 8);
+  DevBuf part;
+  part.alloc((size_t) grid * 16);
+  PCG_CUDA(cudaMemsetAsync(part.p, 0, (size_t) grid * 16, s));
+  k_pairs<<<grid, 256, 0, s>>>(split.as<PairOuter>(), (int64_t) np, c.tab.primes.as<uint32_t>(),
+                               c.tab.pmagic.as<uint64_t>(), c.tab.pibig.as<uint64_t>(), part.as<i128>());
+  PCG_CUDA(cudaGetLastError());
+  if (launches) *launches += 6;
+  return sum_partials(part, grid, s);
 }
 
 struct AcParams {
@@ -862,14 +933,7 @@ static PiParts pi_gourdon(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s)
       if (nC2) k_outer_C2<<<(unsigned) ((nC2 + 127) / 128), 128, 0, s>>>(P, o + nA + nC1 + nQ);
       PCG_CUDA(cudaGetLastError());
       R.launches += 4;
-      const int grid = (int) std::min<int64_t>(nout, (int64_t) c.num_sms * 8);
-      DevBuf part;
-      part.alloc((size_t) grid * 16);
-      PCG_CUDA(cudaMemsetAsync(part.p, 0, (size_t) grid * 16, s));
-      k_pairs<<<grid, 256, 0, s>>>(o, nout, T.primes.as<uint32_t>(), c.tab.pmagic.as<uint64_t>(), T.pibig.as<uint64_t>(), part.as<i128>());
-      PCG_CUDA(cudaGetLastError());
-      R.launches++;
-      sum = sum_partials(part, grid, s);
+      sum = run_pairs(c, o, nout, s, &R.launches);
     }
     R.ac = sum;
     R.ms_ac = fnow_ms() - t1;
@@ -1086,18 +1150,12 @@ int64_t phi_any(Ctx& c, int64_t x, int64_t a, const Tuning& tune, cudaStream_t s
     const int64_t i1 = host_pi(c.tab, (uint64_t) iroot((u128) x, 3));
     if (i1 > a) {
       const int64_t n = i1 - a;
-      DevBuf outs, part;
+      DevBuf outs;
       outs.alloc((size_t) n * sizeof(PairOuter));
       k_outer_P3<<<(unsigned) ((n + 127) / 128), 128, 0, s>>>((uint64_t) x, a, i1, c.tab.primes.as<uint32_t>(),
                                                               c.tab.pibig.as<uint64_t>(), outs.as<PairOuter>());
       PCG_CUDA(cudaGetLastError());
-      const int grid = (int) std::min<int64_t>(n, (int64_t) c.num_sms * 8);
-      part.alloc((size_t) grid * 16);
-      PCG_CUDA(cudaMemsetAsync(part.p, 0, (size_t) grid * 16, s));
-      k_pairs<<<grid, 256, 0, s>>>(outs.as<PairOuter>(), n, c.tab.primes.as<uint32_t>(), c.tab.pmagic.as<uint64_t>(), c.tab.pibig.as<uint64_t>(),
-                                   part.as<i128>());
-      PCG_CUDA(cudaGetLastError());
-      P3 = sum_partials(part, grid, s);
+      P3 = run_pairs(c, outs.as<PairOuter>(), n, s, nullptr);
     }
     return (int64_t) (1 + (i128) (pix - a) + P2 + P3);
   }
