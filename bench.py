@@ -224,6 +224,8 @@ def main():
                     help="queries per kind of the batched workload (4096 = the full config; 0 = skip)")
     ap.add_argument("--plain-sample", type=int, default=24, help="queries per kind timed in the plain form")
     ap.add_argument("--serve-seconds", type=float, default=0, help="serving stream length (0 = skip)")
+    ap.add_argument("--serve-budget", type=float, default=2.0,
+                    help="serving admission budget in estimated GPU-seconds (0 = admit everything)")
     args = ap.parse_args()
     global X
     X = int(float(args.x)) if "e" in args.x else int(args.x)
@@ -348,10 +350,14 @@ def main():
     if args.serve_seconds > 0 and rank == 0:
         from primecount_gb300 import serve as sv
         stream = sv.make_stream(20261203, 2000, args.serve_seconds)
-        r = sv.run_served(stream, workers=4, max_x=10 ** 20, drain_s=30)
+        budget = args.serve_budget if args.serve_budget > 0 else None
+        r = sv.run_served(stream, workers=4, max_x=10 ** 20, drain_s=30, latency_budget=budget)
         r.pop("results")
-        serve = {"served": r, "config": {"rate": 2000, "seconds": args.serve_seconds, "seed": 20261203,
-                                         "pi_x": "10^U(8,20)", "phi_x": "10^U(8,16)", "requests": len(stream)}}
+        plain = sv.run_plain(stream, drain_s=30, latency_budget=budget)
+        serve = {"served": r, "plain": plain,
+                 "config": {"rate": 2000, "seconds": args.serve_seconds, "seed": 20261203,
+                            "pi_x": "10^U(8,20)", "phi_x": "10^U(8,16)", "requests": len(stream),
+                            "latency_budget_s": budget, "workers": 4}}
 
     if rank != 0:
         return

@@ -22,7 +22,8 @@ LIB_PATH = os.path.join(_HERE, "libpcgpu.so")
 
 PCG_OK = 0
 STATUS = {0: "PCG_OK", 1: "PCG_EINVAL", 2: "PCG_ERANGE", 3: "PCG_ENOMEM", 4: "PCG_ECUDA",
-          5: "PCG_ENODEV", 6: "PCG_ETIMEOUT", 7: "PCG_ECANCELLED", 8: "PCG_EINTERNAL"}
+          5: "PCG_ENODEV", 6: "PCG_ETIMEOUT", 7: "PCG_ECANCELLED", 8: "PCG_EINTERNAL",
+          9: "PCG_EAGAIN"}   # 9: refused by the serving loop's latency budget (no C status)
 
 
 class PrimecountError(RuntimeError):

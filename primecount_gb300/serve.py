@@ -4,15 +4,22 @@ A Server keeps `workers` device contexts whose primes, PiTable and
 FactorTable are sized for the largest admitted x and stay resident.  Requests
 wait in one queue; every worker takes the next request as soon as it is free,
 so requests that arrive while others are on the GPU are admitted as slots free
-up and their launches overlap on the device (continuous batching).  A request
-whose x exceeds the admitted maximum is refused at submission (its tables
-would not fit the resident state).  Results are exactly those of a call made
-alone: the workers share no mutable state.
+up and their launches overlap on the device (continuous batching).  Results
+are exactly those of a call made alone: the workers share no mutable state.
+
+Admission.  A request is refused at submission when its x exceeds the
+admitted maximum (its tables would not fit the resident state), and, when a
+latency budget is set, when the GPU-seconds already admitted but not finished
+plus its own estimate exceed the budget (load shedding: under overload the
+admitted requests keep a bounded latency instead of all of them waiting
+behind an unbounded queue).  The estimate is a cost model of the engine on
+one GB300 (`est_seconds`).
 
 The plain comparator runs the same arrivals one request at a time with the
-tables built inside every call (a fresh context per request).
+tables built inside every call (a fresh context per request), under the same
+admission rule.
 
-    python -m primecount_gb300.serve --rate 2000 --seconds 60   # config of record
+    python -m primecount_gb300.serve --rate 2000 --seconds 60 --plain   # config of record
 """
 import argparse
 import collections
@@ -25,32 +32,52 @@ import time
 
 import primecount_gb300 as pcg
 
+PCG_EAGAIN = 9   # refused: the admitted backlog would exceed the latency budget
+
+
+def est_seconds(kind, x, a=None):
+    """GPU-seconds of one query on one GB300 with resident tables (measured:
+    pi(1e16) 0.03 s, pi(1e18) 0.24 s, pi(1e20) 4.2 s; phi(x <= 1e16, a) a few ms)."""
+    x = max(int(x), 2)
+    if kind == "pi":
+        return 0.004 + 4.2 * (x / 1e20) ** 0.6
+    return 0.002 + 0.05 * (x / 1e16) ** 0.5
+
 
 class Request:
-    __slots__ = ("kind", "x", "a", "t_arrival", "t_done", "future")
+    __slots__ = ("kind", "x", "a", "t_arrival", "t_done", "future", "est")
 
     def __init__(self, kind, x, a=None):
         self.kind, self.x, self.a = kind, x, a
         self.t_arrival = time.perf_counter()
         self.t_done = None
         self.future = cf.Future()
+        self.est = est_seconds(kind, x, a)
+
+
+def _compute_pcg(ctx, kind, x, a):
+    return pcg.pi(x, ctx=ctx) if kind == "pi" else pcg.phi(x, a, ctx=ctx)
 
 
 class Server:
-    def __init__(self, max_x=10 ** 20, workers=4, mem_budget=0):
+    def __init__(self, max_x=10 ** 20, workers=4, mem_budget=0, latency_budget=None, compute=None):
         self.max_x = int(max_x)
-        self.ctx = [pcg.Context(self.max_x, mem_budget) for _ in range(workers)]
+        self.budget = latency_budget
+        self.compute = compute or _compute_pcg
+        self.ctx = [pcg.Context(self.max_x, mem_budget) if compute is None else None for _ in range(workers)]
         self.q = collections.deque()
         self.cv = threading.Condition()
         self.stop = False
         self.admitted = 0
-        self.refused = 0
+        self.refused = 0              # above the admitted x
+        self.shed = 0                 # refused by the latency budget
+        self.backlog = 0.0            # estimated GPU-seconds admitted, not finished
         self.threads = [threading.Thread(target=self._work, args=(c,), daemon=True) for c in self.ctx]
         for t in self.threads:
             t.start()
 
     def device_bytes(self):
-        return sum(c.device_bytes() for c in self.ctx)
+        return sum(c.device_bytes() for c in self.ctx if c is not None)
 
     def submit(self, kind, x, a=None):
         r = Request(kind, int(x), None if a is None else int(a))
@@ -59,6 +86,14 @@ class Server:
             r.future.set_exception(pcg.PrimecountError(2, "x above the admitted maximum %d" % self.max_x))
             return r
         with self.cv:
+            cost = r.est
+            if self.budget is not None and self.backlog + cost > self.budget and self.backlog > 0:
+                self.shed += 1
+                r.future.set_exception(pcg.PrimecountError(PCG_EAGAIN, "overloaded: %.2f s of admitted work"
+                                                           % self.backlog))
+                return r
+            r.est = cost
+            self.backlog += cost
             self.admitted += 1
             self.q.append(r)
             self.cv.notify()
@@ -73,12 +108,14 @@ class Server:
                     return
                 r = self.q.popleft()
             try:
-                v = pcg.pi(r.x, ctx=ctx) if r.kind == "pi" else pcg.phi(r.x, r.a, ctx=ctx)
+                v = self.compute(ctx, r.kind, r.x, r.a)
                 r.t_done = time.perf_counter()
                 r.future.set_result(v)
             except Exception as e:  # reported through the future
                 r.t_done = time.perf_counter()
                 r.future.set_exception(e)
+            with self.cv:
+                self.backlog = max(0.0, self.backlog - r.est)
 
     def cancel_pending(self):
         """Drop the queued requests (they fail with PCG_ECANCELLED)."""
@@ -86,6 +123,7 @@ class Server:
             n = len(self.q)
             while self.q:
                 r = self.q.popleft()
+                self.backlog = max(0.0, self.backlog - r.est)
                 r.future.set_exception(pcg.PrimecountError(7, "cancelled"))
         return n
 
@@ -96,7 +134,8 @@ class Server:
         for t in self.threads:
             t.join()
         for c in self.ctx:
-            c.close()
+            if c is not None:
+                c.close()
 
 
 def pi_upper(x):
@@ -106,10 +145,10 @@ def pi_upper(x):
     return int(1.25506 * x / math.log(x)) + 1
 
 
-def make_stream(seed, rate, seconds, pi_range=(8, 20), phi_range=(8, 16), pi_frac=0.5):
+def make_stream(seed, rate, seconds, pi_range=(8, 20), phi_range=(8, 16), pi_frac=0.5, pi_of=None):
     """Poisson arrivals of mixed pi / phi requests from a seeded generator.
     a is uniform in [1, pi(sqrt x)] (pi computed for the small sqrt(x) by the
-    engine itself)."""
+    engine itself, or by pi_of)."""
     rng = random.Random(seed)
     t = 0.0
     out = []
@@ -124,7 +163,10 @@ def make_stream(seed, rate, seconds, pi_range=(8, 20), phi_range=(8, 16), pi_fra
             out.append((t, "phi", x, rng.random()))
     # resolve a = U{1, pi(sqrt x)} with exact pi(sqrt x)
     sq = sorted({int(math.isqrt(x)) for _, k, x, _ in out if k == "phi"})
-    pis = dict(zip(sq, pcg.pi_batch(sq))) if sq else {}
+    if sq:
+        pis = dict(zip(sq, pi_of(sq) if pi_of else pcg.pi_batch(sq)))
+    else:
+        pis = {}
     res = []
     for t, k, x, u in out:
         if k == "phi":
@@ -143,8 +185,8 @@ def percentile(v, q):
     return v[i]
 
 
-def run_served(stream, workers=4, max_x=10 ** 20, drain_s=30.0):
-    srv = Server(max_x=max_x, workers=workers)
+def run_served(stream, workers=4, max_x=10 ** 20, drain_s=30.0, latency_budget=None, compute=None):
+    srv = Server(max_x=max_x, workers=workers, latency_budget=latency_budget, compute=compute)
     t0 = time.perf_counter()
     reqs = []
     for (t, k, x, a) in stream:
@@ -154,7 +196,6 @@ def run_served(stream, workers=4, max_x=10 ** 20, drain_s=30.0):
         reqs.append(srv.submit(k, x, a))
     t_end_arrivals = time.perf_counter()
     deadline = t_end_arrivals + drain_s
-    done = [r for r in reqs if r.future.done()]
     for r in reqs:
         rem = deadline - time.perf_counter()
         if rem <= 0:
@@ -168,38 +209,51 @@ def run_served(stream, workers=4, max_x=10 ** 20, drain_s=30.0):
     srv.close()
     ok = [r for r in reqs if r.future.done() and not r.future.exception()]
     lat = [r.t_done - r.t_arrival for r in ok]
-    return {"completed": len(ok), "submitted": len(reqs), "cancelled_at_deadline": cancelled,
-            "refused": srv.refused, "wall_s": t_stop - t0, "qps": len(ok) / (t_stop - t0),
+    return {"completed": len(ok), "submitted": len(reqs), "admitted": srv.admitted,
+            "shed_by_budget": srv.shed, "refused_above_max_x": srv.refused,
+            "cancelled_at_deadline": cancelled, "wall_s": t_stop - t0, "qps": len(ok) / (t_stop - t0),
             "p50_s": percentile(lat, 0.5), "p99_s": percentile(lat, 0.99),
             "results": {id(r): r.future.result() for r in ok}}
 
 
-def run_plain(stream, drain_s=30.0, seconds=None):
-    """One request at a time, tables built inside every call."""
+def run_plain(stream, drain_s=30.0, latency_budget=None, compute=None):
+    """One request at a time, tables built inside every call; the same
+    admission rule (budget on the estimated GPU-seconds waiting)."""
     t0 = time.perf_counter()
     lat = []
-    n = 0
+    n = shed = 0
     pending = collections.deque()
+    backlog = 0.0
     i = 0
     limit = (stream[-1][0] if stream else 0) + drain_s
     while i < len(stream) or pending:
         now = time.perf_counter() - t0
         while i < len(stream) and stream[i][0] <= now:
-            pending.append(stream[i])
+            t, k, x, a = stream[i]
+            e = est_seconds(k, x, a)
+            if latency_budget is not None and backlog + e > latency_budget and backlog > 0:
+                shed += 1
+            else:
+                pending.append((t, k, x, a, e))
+                backlog += e
             i += 1
         if not pending:
             time.sleep(max(0.0, stream[i][0] - now))
             continue
         if now > limit:
             break
-        t, k, x, a = pending.popleft()
-        c = pcg.Context(0)
-        v = pcg.pi(x, ctx=c) if k == "pi" else pcg.phi(x, a, ctx=c)
-        c.close()
+        t, k, x, a, e = pending.popleft()
+        if compute is None:
+            c = pcg.Context(0)
+            v = _compute_pcg(c, k, x, a)
+            c.close()
+        else:
+            compute(None, k, x, a)
+        backlog = max(0.0, backlog - e)
         lat.append(time.perf_counter() - t0 - t)
         n += 1
     wall = time.perf_counter() - t0
-    return {"completed": n, "submitted": len(stream), "wall_s": wall, "qps": n / wall,
+    return {"completed": n, "submitted": len(stream), "shed_by_budget": shed, "wall_s": wall, "qps": n / wall,
             "p50_s": percentile(lat, 0.5), "p99_s": percentile(lat, 0.99)}
 
 
@@ -212,16 +266,20 @@ def main():
     ap.add_argument("--max-x", default="1e20")
     ap.add_argument("--pi-max-exp", type=float, default=20)
     ap.add_argument("--drain", type=float, default=30)
+    ap.add_argument("--budget", type=float, default=2.0,
+                    help="latency budget in estimated GPU-seconds of admitted work (0 = admit everything)")
     ap.add_argument("--plain", action="store_true")
     a = ap.parse_args()
+    budget = a.budget if a.budget > 0 else None
     stream = make_stream(a.seed, a.rate, a.seconds, pi_range=(8, a.pi_max_exp))
     out = {"config": {"rate": a.rate, "seconds": a.seconds, "seed": a.seed, "workers": a.workers,
-                      "pi_x": "10^U(8,%g)" % a.pi_max_exp, "phi_x": "10^U(8,16)", "requests": len(stream)}}
-    r = run_served(stream, workers=a.workers, max_x=int(float(a.max_x)), drain_s=a.drain)
+                      "pi_x": "10^U(8,%g)" % a.pi_max_exp, "phi_x": "10^U(8,16)", "requests": len(stream),
+                      "latency_budget_s": budget}}
+    r = run_served(stream, workers=a.workers, max_x=int(float(a.max_x)), drain_s=a.drain, latency_budget=budget)
     r.pop("results")
     out["served"] = r
     if a.plain:
-        out["plain"] = run_plain(stream, drain_s=a.drain)
+        out["plain"] = run_plain(stream, drain_s=a.drain, latency_budget=budget)
     print(json.dumps(out))
 
 
