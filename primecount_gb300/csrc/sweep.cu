@@ -329,6 +329,7 @@ struct SweepArgs {
   int64_t* segsum;          // [wave_len]
   unsigned long long* counters;  // [0] leaves, [1] two-prime leaves, [2] levels, [3] factor entries
   int* queue;
+  int group_max;            // levels answered together (<= GROUP_MAX; < 2: off)
 };
 
 // primes 7..61 sieved with wheel patterns (their multiples repeat every p words)
@@ -407,6 +408,8 @@ __device__ __forceinline__ uint32_t query(const uint64_t* __restrict__ bits, con
 // Record of one table entry: the offset of the leaf in the segment, bit 30 =
 // negative sign, or REC_NONE when the factor-table filter rejects the entry.
 #define REC_NONE 0xFFFFFFFFu
+// consecutive levels with p^3 >= high answered together (see k_sweep)
+#define GROUP_MAX 64
 // x / (p m) through the reciprocal of m when x / p < 2^64
 template <typename FT>
 __device__ __forceinline__ uint32_t make_record(const SweepArgs& A, const LevelP& P, int64_t e, uint32_t fv,
@@ -468,9 +471,11 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
   uint32_t* rec = (uint32_t*) (lp + NT);
   uint16_t* runend = (uint16_t*) (rec + A.rec_cap);    // end of the run of leafless levels from i
   uint16_t* cop = runend + NT;
+  uint32_t* s_pc = (uint32_t*) (((uintptr_t) (cop + 480) + 3) & ~(uintptr_t) 3);   // pi(q_lo - 1) of flag-8 levels
 
   __shared__ int s_ws;
   __shared__ uint32_t wtmp[32];
+  __shared__ int s_gsmu[GROUP_MAX];                    // signed leaf counts of a level group
   __shared__ int s_smu;
   __shared__ int s_stop;
   __shared__ uint32_t s_rem[3];
@@ -569,6 +574,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
         const int b = b0 + tid;
         LevelP P;
         P.lo = P.hi = 0; P.jlo = 0; P.jn = 0; P.prime = 0; P.thr = 0; P.flags = 0; P.level = b; P.fcount = 0;
+        uint32_t pcv = 0;
         if (b <= Bs) {
           const uint64_t p = A.primes[b];
           P.prime = (uint32_t) p;
@@ -586,9 +592,11 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
             if ((u128) p * p * p >= (u128) high && (int64_t) qhi <= A.pi_max) {
               uint32_t f = ((uint64_t) low <= p && p < (uint64_t) high) ? 1u : 0u;
               const uint64_t qa = qlo > p ? qlo : p;
-              if (qhi >= qa) f += (uint32_t) (dpi(A.pitab, qhi) - dpi(A.pitab, qa - 1));
+              const int64_t pc = dpi(A.pitab, qa - 1);
+              if (qhi >= qa) f += (uint32_t) (dpi(A.pitab, qhi) - pc);
               P.fcount = f;
               P.flags |= 8;
+              pcv = (uint32_t) pc;
             }
           } else if (p >= 7) {
             P.jlo = (uint64_t) ((low / 240) % p);   // pattern phase of the first word
@@ -651,6 +659,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
         }
         fcnt = P.fcount;
         lp[tid] = P;
+        s_pc[tid] = pcv;
       }
       __syncthreads();
       const int nb = (int) dmin(NT, (int64_t) (Bs - b0 + 1));
@@ -767,6 +776,80 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
             li = re;
             __syncthreads();
             continue;
+          }
+          // ---- levels li .. lj-1 with p^3 >= high whose records all lie in this
+          // window: the numbers such a level removes are p and the p q with
+          // prime q >= p, so the count at level l of a record's n is the count
+          // at level li minus sum_{li <= b < l} ([low <= p_b <= n] +
+          // pi(n / p_b) - pi(q_lo_b - 1)).  All their records are answered
+          // against one bitmap state, then all their multiples crossed off at
+          // once: one barrier pass instead of one per level.
+          if ((lp[li].flags & 8) && loff[li] >= w0) {
+            int lj = li;
+            while (lj < nb && lj - li < A.group_max && (lp[lj].flags & 8) && loff[lj + 1] <= wend) lj++;
+            if (lj - li >= 2) {
+              const int ra = (int) (loff[li] - w0), rb = (int) (loff[lj] - w0);
+              if (tid < lj - li) s_gsmu[tid] = 0;
+              if (rb > ra && dirty) { scan_chunks(ccount, pref, nch, wtmp); dirty = false; }
+              else __syncthreads();
+              if (rb > ra) {
+                int lv = li;
+                for (int k2 = ra + tid; k2 < rb; k2 += NT) {
+                  const int64_t pos = w0 + k2;
+                  while (loff[lv + 1] <= pos) lv++;
+                  const uint32_t r = rec[k2];
+                  int sg = 0;
+                  if (r != REC_NONE) {
+                    const uint32_t off = r & 0x3FFFFFFFu;
+                    uint32_t c = query(bits, pref, off);
+                    const uint64_t n = (uint64_t) low + off;
+                    for (int b = li; b < lv; b++) {
+                      const uint64_t pb = lp[b].prime;
+                      if (pb <= n && pb >= (uint64_t) low) c--;
+                      const int64_t d = dpi(A.pitab, div_magic(n, pb, A.pmagic[b0 + b])) - (int64_t) s_pc[b];
+                      if (d > 0) c -= (uint32_t) d;
+                    }
+                    if (r & (1u << 30)) { lsum -= c; sg = -1; }
+                    else { lsum += c; sg = 1; }
+                  }
+                  // signed counts per level, aggregated over the lanes of one level
+                  const unsigned act = __activemask();
+                  const unsigned same = __match_any_sync(act, lv);
+                  const int tot = __reduce_add_sync(same, sg);
+                  if (tot && lane == __ffs((int) same) - 1) atomicAdd(&s_gsmu[lv - li], tot);
+                }
+              }
+              __syncthreads();
+              // the levels' counts C(s, b) and signed leaf counts M(s, b)
+              const int64_t r0 = rpre[li];
+              for (int t = tid; t < lj - li; t += NT) {
+                const int64_t cell = (int64_t) ws * cols + b0 + li + t;
+                A.cnt[cell] = total - (uint32_t) (rpre[li + t] - r0);
+                if (s_gsmu[t]) A.smu[cell] = s_gsmu[t];
+              }
+              // all their multiples crossed off at once
+              const int64_t h0 = hoff[li], h1 = hoff[lj];
+              for (int64_t h = h0 + tid; h < h1; h += NT) {
+                int lo = li, hi = lj - 1;       // last level with hoff <= h
+                while (lo < hi) {
+                  const int mid = (lo + hi + 1) >> 1;
+                  if (hoff[mid] <= h) lo = mid; else hi = mid - 1;
+                }
+                const LevelP& Q = lp[lo];
+                const uint64_t jj = Q.jlo + (uint64_t) (h - hoff[lo]);
+                const uint64_t q = 30 * (jj >> 3) + woff((uint32_t) (jj & 7));
+                const uint32_t off = (uint32_t) ((uint64_t) Q.prime * q - (uint64_t) low);
+                const uint32_t w = off / 240, rr = off - w * 240;
+                const uint64_t m = 1ull << bit_of(rr);
+                const uint64_t old = atomicAnd((unsigned long long*) &bits[w], ~m);
+                if (old & m) atomicSub(&ccount[w >> 3], 1u);
+              }
+              total -= (uint32_t) (rpre[lj] - r0);
+              if (h1 > h0) dirty = true;
+              li = lj;
+              __syncthreads();
+              continue;
+            }
           }
           const int64_t la = loff[li], lz = loff[li + 1];
           if (lz > la && la >= wend) break;               // records start in a later window
@@ -1305,6 +1388,17 @@ static std::vector<int64_t> plan_segments(const SweepProblem& pb, const Tables& 
   return seg;
 }
 
+// levels with p^3 >= high answered in one pass (PCG_SWEEP_GROUP overrides)
+static int sweep_group_max()
+{
+  static const int g = [] {
+    const char* e = getenv("PCG_SWEEP_GROUP");
+    const int v = e ? atoi(e) : 16;
+    return v < 0 ? 0 : (v > GROUP_MAX ? GROUP_MAX : v);
+  }();
+  return g;
+}
+
 // ---- checkpoint / resume of a sweep: the phi-offset totals run[b], the leaf
 // sums acc[b] and msum[b] after the last finished wave, with the problem and
 // a hash of the segment plan they belong to
@@ -1432,9 +1526,9 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   const int wq = std::max(8 * NT, 2048);   // whole chunks per thread and per scan lane pair
   words = std::max(words, wq);
   words = (words + wq - 1) / wq * wq;
-  const int cap = 4096;
+  const int cap = 3584;
   size_t smem = (size_t) words * 8 + PAT_WORDS * 8 + (size_t) (NT + 1) * 8 * 3 + (size_t) (words / 8) * 8 +
-                sizeof(LevelP) * NT + (size_t) cap * 4 + (size_t) NT * 2 + 480 * 2 + 32;
+                sizeof(LevelP) * NT + (size_t) cap * 4 + (size_t) NT * 2 + 480 * 2 + (size_t) NT * 4 + 32;
   if (smem > c.smem_optin) fail(PCG_EINVAL, "segment too large for shared memory");
   int fbytes = pb.gourdon ? c.tab.fd_bytes : c.tab.fr_bytes;
   auto occupancy = [&](int* occ) {
@@ -1508,6 +1602,7 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   a.factor = pb.gourdon ? c.tab.factor_d.p : c.tab.factor_dr.p;
   a.xp_tab = d_xp;
   a.coprime = c.tab.coprime.as<uint16_t>();
+  a.group_max = sweep_group_max();
   a.cindex = c.tab.cindex.as<int16_t>();
   a.finv = c.tab.finv.as<uint64_t>();
   a.pmagic = c.tab.pmagic.as<uint64_t>();
@@ -1809,9 +1904,9 @@ SweepResult run_sweep_noalloc(Ctx& c, const SweepProblem& pb, cudaStream_t s)
 
   const int NT = 256;
   const int words = 8192;
-  const int cap = 4096;
+  const int cap = 3584;
   size_t smem = (size_t) words * 8 + PAT_WORDS * 8 + (size_t) (NT + 1) * 8 * 3 + (size_t) (words / 8) * 8 +
-                sizeof(LevelP) * NT + (size_t) cap * 4 + (size_t) NT * 2 + 480 * 2 + 32;
+                sizeof(LevelP) * NT + (size_t) cap * 4 + (size_t) NT * 2 + 480 * 2 + (size_t) NT * 4 + 32;
   const int fbytes = T.fd_bytes;
   int occ = 0;
   if (fbytes == 2) occupancy_sweep<uint16_t, 256>(&occ, smem);
@@ -1881,6 +1976,7 @@ SweepResult run_sweep_noalloc(Ctx& c, const SweepProblem& pb, cudaStream_t s)
   a.factor = T.factor_d.p;
   a.xp_tab = d_xp;
   a.coprime = T.coprime.as<uint16_t>();
+  a.group_max = sweep_group_max();
   a.cindex = T.cindex.as<int16_t>();
   a.finv = T.finv.as<uint64_t>();
   a.pmagic = T.pmagic.as<uint64_t>();
