@@ -393,46 +393,32 @@ __device__ __forceinline__ void scan_chunks(const uint32_t* __restrict__ ccount,
   __syncthreads();
 }
 
-// # unsieved numbers in [low, low + off]
+// # unsieved numbers in [low, low + off]: the chunk prefix plus the popcounts
+// of the chunk's words up to the word of off, its 8 words read at once
 __device__ __forceinline__ uint32_t query(const uint64_t* __restrict__ bits, const uint32_t* __restrict__ pref,
                                           uint32_t off)
 {
   const uint32_t w = off / 240;
   const uint32_t r = off - w * 240;
   const uint32_t c = w >> 3;
-  uint32_t v = pref[c];
-  for (uint32_t i = c << 3; i < w; i++) v += __popcll(bits[i]);
-  return v + __popcll(bits[w] & mask_le(r));
+  const uint32_t k = w & 7;
+  const ulonglong2* q = (const ulonglong2*) (bits + (c << 3));
+  const ulonglong2 w01 = q[0], w23 = q[1], w45 = q[2], w67 = q[3];
+  const uint64_t mk = mask_le(r);
+  auto part = [&](uint32_t i, uint64_t v) -> uint32_t {
+    return (uint32_t) __popcll(i < k ? v : (i == k ? (v & mk) : 0ull));
+  };
+  return pref[c] + part(0, w01.x) + part(1, w01.y) + part(2, w23.x) + part(3, w23.y) + part(4, w45.x) +
+         part(5, w45.y) + part(6, w67.x) + part(7, w67.y);
 }
 
 // Record of one table entry: the offset of the leaf in the segment, bit 30 =
 // negative sign, or REC_NONE when the factor-table filter rejects the entry.
 #define REC_NONE 0xFFFFFFFFu
+// table entries per thread and round of the record phase
+#define PA_UNROLL 8
 // consecutive levels with p^3 >= high answered together (see k_sweep)
 #define GROUP_MAX 64
-// x / (p m) through the reciprocal of m when x / p < 2^64
-template <typename FT>
-__device__ __forceinline__ uint32_t make_record(const SweepArgs& A, const LevelP& P, int64_t e, uint32_t fv,
-                                                const uint16_t* __restrict__ cop, uint64_t low)
-{
-  const uint64_t* xt = A.xp_tab + 3 * (int64_t) P.level;
-  const uint64_t xlo = xt[0], xhi = xt[1];
-  const int64_t idx = P.hi - e;
-  if (!(P.flags & 2)) {
-    if (fv <= P.thr) return REC_NONE;
-    uint64_t m;
-    if ((uint64_t) idx <= 0xFFFFFFFFull) {
-      const uint32_t mi = (uint32_t) idx;
-      m = 2310ull * (mi / 480u) + cop[mi % 480u];
-    } else {
-      m = 2310ull * ((uint64_t) idx / 480) + cop[(uint64_t) idx % 480];
-    }
-    const uint64_t nn = xhi == 0 ? div_magic(xlo, m, __ldg(&A.finv[idx])) : div_xp(xlo, xhi, m);
-    return (uint32_t) (nn - low) | ((fv & 1) ? 0u : (1u << 30));
-  }
-  const uint64_t nn = xhi == 0 ? div_magic(xlo, fv, __ldg(&A.pmagic[idx])) : div_xp(xlo, xhi, (uint64_t) fv);
-  return (uint32_t) (nn - low);
-}
 
 // exclusive block scan of three int64 values per thread into out[NT + 1] arrays
 template <int NT>
@@ -692,18 +678,22 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
       int64_t w0 = 0;      // first flat record of the window
       while (li < nb) {
         const int64_t wend = w0 + cap;
-        // ---- phase A: the window's leaf records (flat over levels, 4 loads in flight)
+        // ---- phase A: the window's leaf records, flat over levels, PA_UNROLL
+        // entries per thread in three stages so that their table loads, then
+        // their reciprocal loads, are in flight together
         const int nrec = (int) dmax(0, dmin(wend, total_e) - w0);
         if (nrec > 0) {
           int lv = li;       // level of this thread's previous entry
-          for (int f0 = tid; f0 < nrec; f0 += 4 * NT) {
-            int jl[4];
-            int64_t el[4];
-            uint32_t fv[4];
+          for (int f0 = tid; f0 < nrec; f0 += PA_UNROLL * NT) {
+            int jl[PA_UNROLL];
+            int el[PA_UNROLL];
+            uint32_t fv[PA_UNROLL];
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
+            for (int u = 0; u < PA_UNROLL; u++) {
               const int f = f0 + u * NT;
               jl[u] = -1;
+              el[u] = 0;
+              fv[u] = 0;
               if (f < nrec) {
                 const int64_t pos = w0 + f;
                 // last level with loff <= pos: a few steps forward from the
@@ -720,19 +710,53 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                 }
                 lv = lo;
                 jl[u] = lo;
-                el[u] = pos - loff[lo];
+                el[u] = (int) (pos - loff[lo]);
                 const LevelP& Q = lp[lo];
                 fv[u] = (Q.flags & 2) ? __ldg(&A.primes[Q.hi - el[u]]) : (uint32_t) __ldg(&factor[Q.hi - el[u]]);
               }
             }
+            // the divisor m of each accepted entry (0: rejected by the
+            // factor-table filter) and its reciprocal
+            uint64_t mdiv[PA_UNROLL], minv[PA_UNROLL];
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
+            for (int u = 0; u < PA_UNROLL; u++) {
+              mdiv[u] = 0;
+              minv[u] = 0;
+              if (jl[u] >= 0) {
+                const LevelP& Q = lp[jl[u]];
+                const int64_t idx = Q.hi - el[u];
+                if (Q.flags & 2) {
+                  mdiv[u] = fv[u];
+                  minv[u] = __ldg(&A.pmagic[idx]);
+                } else if (fv[u] > Q.thr) {
+                  if ((uint64_t) idx <= 0xFFFFFFFFull) {
+                    const uint32_t mi = (uint32_t) idx;
+                    mdiv[u] = 2310ull * (mi / 480u) + cop[mi % 480u];
+                  } else {
+                    mdiv[u] = 2310ull * ((uint64_t) idx / 480) + cop[(uint64_t) idx % 480];
+                  }
+                  minv[u] = __ldg(&A.finv[idx]);
+                }
+              }
+            }
+            // n = (x / p) / m, the record: offset in the segment, bit 30 for
+            // the negative sign of -mu(m) (an even factor-table entry)
+#pragma unroll
+            for (int u = 0; u < PA_UNROLL; u++) {
               const int f = f0 + u * NT;
               if (jl[u] >= 0) {
                 const LevelP& Q = lp[jl[u]];
-                const uint32_t r = make_record<FT>(A, Q, el[u], fv[u], cop, (uint64_t) low);
+                uint32_t r = REC_NONE;
+                if (mdiv[u]) {
+                  const uint64_t* xt = A.xp_tab + 3 * (int64_t) Q.level;
+                  const uint64_t xlo = xt[0], xhi = xt[1];
+                  const uint64_t nn = xhi == 0 ? div_magic(xlo, mdiv[u], minv[u]) : div_xp(xlo, xhi, mdiv[u]);
+                  r = (uint32_t) (nn - (uint64_t) low);
+                  if (!(Q.flags & 2) && !(fv[u] & 1)) r |= 1u << 30;
+                  nleaves++;
+                  if (Q.flags & 2) ntwo++;
+                }
                 rec[f] = r;
-                if (r != REC_NONE) { nleaves++; if (Q.flags & 2) ntwo++; }
               }
             }
           }
