@@ -711,23 +711,36 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                 lv = lo;
                 jl[u] = lo;
                 el[u] = (int) (pos - loff[lo]);
-                const LevelP& Q = lp[lo];
-                fv[u] = (Q.flags & 2) ? __ldg(&A.primes[Q.hi - el[u]]) : (uint32_t) __ldg(&factor[Q.hi - el[u]]);
               }
             }
-            // the divisor m of each accepted entry (0: rejected by the
-            // factor-table filter) and its reciprocal
+            // table entries and the reciprocals of their divisors, loaded
+            // together (the reciprocal of a rejected entry goes unused)
             uint64_t mdiv[PA_UNROLL], minv[PA_UNROLL];
 #pragma unroll
             for (int u = 0; u < PA_UNROLL; u++) {
-              mdiv[u] = 0;
               minv[u] = 0;
               if (jl[u] >= 0) {
                 const LevelP& Q = lp[jl[u]];
                 const int64_t idx = Q.hi - el[u];
                 if (Q.flags & 2) {
-                  mdiv[u] = fv[u];
+                  fv[u] = __ldg(&A.primes[idx]);
                   minv[u] = __ldg(&A.pmagic[idx]);
+                } else {
+                  fv[u] = (uint32_t) __ldg(&factor[idx]);
+                  minv[u] = __ldg(&A.finv[idx]);
+                }
+              }
+            }
+            // the divisor m of each accepted entry (0: rejected by the
+            // factor-table filter)
+#pragma unroll
+            for (int u = 0; u < PA_UNROLL; u++) {
+              mdiv[u] = 0;
+              if (jl[u] >= 0) {
+                const LevelP& Q = lp[jl[u]];
+                const int64_t idx = Q.hi - el[u];
+                if (Q.flags & 2) {
+                  mdiv[u] = fv[u];
                 } else if (fv[u] > Q.thr) {
                   if ((uint64_t) idx <= 0xFFFFFFFFull) {
                     const uint32_t mi = (uint32_t) idx;
@@ -735,7 +748,6 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                   } else {
                     mdiv[u] = 2310ull * ((uint64_t) idx / 480) + cop[(uint64_t) idx % 480];
                   }
-                  minv[u] = __ldg(&A.finv[idx]);
                 }
               }
             }
