@@ -682,7 +682,66 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
         // entries per thread in three stages so that their table loads, then
         // their reciprocal loads, are in flight together
         const int nrec = (int) dmax(0, dmin(wend, total_e) - w0);
-        if (nrec > 0) {
+        // a window inside one level (the dense case): that level's constants
+        // held in registers, no level lookup per entry
+        const bool one_level = nrec > 0 && loff[li] <= w0 && loff[li + 1] >= w0 + nrec;
+        if (one_level) {
+          const LevelP& Q = lp[li];
+          const int64_t hi0 = Q.hi - (w0 - loff[li]);        // table index of entry f is hi0 - f
+          const bool two = (Q.flags & 2) != 0;
+          const uint32_t thr = Q.thr;
+          const uint64_t* xt = A.xp_tab + 3 * (int64_t) Q.level;
+          const uint64_t xlo = xt[0], xhi = xt[1];
+          unsigned nl = 0;
+          for (int f0 = tid; f0 < nrec; f0 += PA_UNROLL * NT) {
+            uint32_t fv[PA_UNROLL];
+            uint64_t minv[PA_UNROLL];
+#pragma unroll
+            for (int u = 0; u < PA_UNROLL; u++) {
+              const int f = f0 + u * NT;
+              fv[u] = 0;
+              minv[u] = 0;
+              if (f < nrec) {
+                const int64_t idx = hi0 - f;
+                if (two) {
+                  fv[u] = __ldg(&A.primes[idx]);
+                  minv[u] = __ldg(&A.pmagic[idx]);
+                } else {
+                  fv[u] = (uint32_t) __ldg(&factor[idx]);
+                  minv[u] = __ldg(&A.finv[idx]);
+                }
+              }
+            }
+#pragma unroll
+            for (int u = 0; u < PA_UNROLL; u++) {
+              const int f = f0 + u * NT;
+              if (f < nrec) {
+                const int64_t idx = hi0 - f;
+                uint64_t m = 0;
+                if (two) m = fv[u];
+                else if (fv[u] > thr) {
+                  if ((uint64_t) idx <= 0xFFFFFFFFull) {
+                    const uint32_t mi = (uint32_t) idx;
+                    m = 2310ull * (mi / 480u) + cop[mi % 480u];
+                  } else {
+                    m = 2310ull * ((uint64_t) idx / 480) + cop[(uint64_t) idx % 480];
+                  }
+                }
+                uint32_t r = REC_NONE;
+                if (m) {
+                  const uint64_t nn = xhi == 0 ? div_magic(xlo, m, minv[u]) : div_xp(xlo, xhi, m);
+                  r = (uint32_t) (nn - (uint64_t) low);
+                  if (!two && !(fv[u] & 1)) r |= 1u << 30;
+                  nl++;
+                }
+                rec[f] = r;
+              }
+            }
+          }
+          nleaves += nl;
+          if (two) ntwo += nl;
+        }
+        if (nrec > 0 && !one_level) {
           int lv = li;       // level of this thread's previous entry
           for (int f0 = tid; f0 < nrec; f0 += PA_UNROLL * NT) {
             int jl[PA_UNROLL];
@@ -772,6 +831,8 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
               }
             }
           }
+        }
+        if (nrec > 0) {
           if (tid == 0) {
             for (int j = li; j < nb; j++) {
               const int64_t a = dmax(loff[j], w0), e2 = dmin(loff[j + 1], wend);
