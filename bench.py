@@ -118,7 +118,7 @@ def cpu_baseline(p, threads, target_s=12.0):
     frac = 1e-4
     leaves, secs = oracle.D_sample(X, p["y"], p["z"], p["k"], nchunks, frac, threads)
     spent = secs
-    while secs < target_s / 6 and frac < 0.05:
+    while secs < target_s * 2 / 3 and frac < 0.05:
         step = min(10.0 if secs < 0.3 else 2.0, 0.8 * target_s / max(secs, 1e-3))
         frac = min(0.05, frac * step)
         leaves, secs = oracle.D_sample(X, p["y"], p["z"], p["k"], nchunks, frac, threads)
