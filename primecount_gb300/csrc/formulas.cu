@@ -189,28 +189,31 @@ static __device__ __forceinline__ long long pi_pt(const ulonglong2* __restrict__
 }
 
 template <int MODE>
-__device__ __forceinline__ long long pair_term(const PairOuter& O, int64_t i, uint32_t q, uint64_t m,
+__device__ __forceinline__ long long pair_term(const PairOuter& O, uint32_t i, uint32_t q, uint64_t m,
                                               const ulonglong2* __restrict__ pt, const uint64_t* s_mask)
 {
   uint64_t n;
   if (O.xp_hi == 0) n = div_magic(O.xp_lo, q, m);
   else n = (uint64_t) ((((u128) O.xp_hi << 64) | O.xp_lo) / q);
-  const long long pin = n < 6 ? (long long) ((0x322100u >> (4 * n)) & 15u) : pi_pt(pt, s_mask, n);
+  // A: n = x / (p q) >= q > 6; the C and P3 terms can reach n < 6
+  const long long pin = (MODE != 0 && n < 6) ? (long long) ((0x322100u >> (4 * n)) & 15u) : pi_pt(pt, s_mask, n);
   if (MODE == 0) return (q <= O.cap) ? pin : 2 * pin;
   if (MODE == 1) return pin - O.b + 2;
   if (MODE == 2) return -(pin - O.b + 2);
-  return pin - i + 1;
+  return pin - (long long) i + 1;
 }
 
-// the terms of one outer, 256 threads, four terms per thread in flight
+// the terms of one outer (prime indices < 2^32), 256 threads, four terms per
+// thread in flight
 template <int MODE>
 __device__ __forceinline__ long long pair_terms(const PairOuter& O, const uint32_t* __restrict__ primes,
                                                 const uint64_t* __restrict__ magic,
                                                 const ulonglong2* __restrict__ pt, const uint64_t* s_mask)
 {
   long long s = 0;
-  int64_t i = O.i_lo + 1 + threadIdx.x;
-  for (; i + 3 * 256 <= O.i_hi; i += 4 * 256) {
+  const uint32_t hi = (uint32_t) O.i_hi;
+  uint32_t i = (uint32_t) (O.i_lo + 1) + threadIdx.x;
+  for (; i + 3 * 256 <= hi; i += 4 * 256) {
     uint32_t q[4];
     uint64_t m[4];
 #pragma unroll
@@ -218,7 +221,7 @@ __device__ __forceinline__ long long pair_terms(const PairOuter& O, const uint32
 #pragma unroll
     for (int u = 0; u < 4; u++) s += pair_term<MODE>(O, i + 256 * u, q[u], m[u], pt, s_mask);
   }
-  for (; i <= O.i_hi; i += 256) s += pair_term<MODE>(O, i, primes[i], magic[i], pt, s_mask);
+  for (; i <= hi; i += 256) s += pair_term<MODE>(O, i, primes[i], magic[i], pt, s_mask);
   return s;
 }
 
