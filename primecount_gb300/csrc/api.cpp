@@ -334,13 +334,20 @@ const char* pcg_last_error(const pcg_ctx* c)
   return tl_error.c_str();
 }
 
+static uint64_t tmp_bytes(const Ctx& c)
+{
+  uint64_t t = 0;
+  for (const DevBuf& b : c.tmp) t += b.bytes;
+  return t;
+}
+
 uint64_t pcg_ctx_device_bytes(const pcg_ctx* c)
 {
   if (!c) return 0;
   const Tables& t = c->tab;
   return t.primes.bytes + t.pitab.bytes + t.factor_d.bytes + t.factor_dr.bytes + t.coprime.bytes + t.cindex.bytes +
          t.pibig.bytes + t.pmagic.bytes + t.phi_bits.bytes + t.phi_pref.bytes + c->cnt.bytes + c->smu.bytes +
-         c->segsum.bytes + c->run.bytes + c->acc.bytes + c->misc.bytes;
+         c->segsum.bytes + c->run.bytes + c->acc.bytes + c->misc.bytes + c->msum.bytes + tmp_bytes(*c);
 }
 
 pcg_status pcg_last_stats(const pcg_ctx* c, pcg_stats* out)

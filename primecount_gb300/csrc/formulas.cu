@@ -278,23 +278,24 @@ __global__ void __launch_bounds__(256) k_pairs(const PairOuter* __restrict__ out
 static i128 run_pairs(Ctx& c, const PairOuter* outs, int64_t nout, cudaStream_t s, uint64_t* launches)
 {
   if (nout <= 0) return 0;
-  DevBuf pieces, first;
+  DevBuf& pieces = c.tmp[T_PR_PIECES];
+  DevBuf& first = c.tmp[T_PR_FIRST];
   pieces.alloc((size_t) (nout + 1) * 4);
   first.alloc((size_t) (nout + 1) * 8);
   k_pair_pieces<<<(unsigned) ((nout + 256) / 256), 256, 0, s>>>(outs, nout, pieces.as<uint32_t>());
   PCG_CUDA(cudaGetLastError());
-  exclusive_scan_u32(pieces.as<uint32_t>(), nout + 1, first.as<uint64_t>(), s);
+  exclusive_scan_u32(pieces.as<uint32_t>(), nout + 1, first.as<uint64_t>(), s, &c.tmp[T_PR_SUMS]);
   uint64_t np = 0;
   PCG_CUDA(cudaMemcpyAsync(&np, first.as<uint64_t>() + nout, 8, cudaMemcpyDeviceToHost, s));
   PCG_CUDA(cudaStreamSynchronize(s));
   if (np == 0) return 0;
-  DevBuf split;
+  DevBuf& split = c.tmp[T_PR_SPLIT];
   split.alloc((size_t) np * sizeof(PairOuter));
   k_pair_split<<<(unsigned) ((nout + 127) / 128), 128, 0, s>>>(outs, nout, first.as<uint64_t>(),
                                                                split.as<PairOuter>());
   PCG_CUDA(cudaGetLastError());
   const int grid = (int) std::min<uint64_t>(np, (uint64_t) c.num_sms * 8);
-  DevBuf part;
+  DevBuf& part = c.tmp[T_PR_PART];
   part.alloc((size_t) grid * 16);
   PCG_CUDA(cudaMemsetAsync(part.p, 0, (size_t) grid * 16, s));
   k_pairs<<<grid, 256, 0, s>>>(split.as<PairOuter>(), (int64_t) np, c.tab.primes.as<uint32_t>(),
@@ -741,7 +742,12 @@ static PsOut run_psieve(Ctx& c, u128 x, int64_t lo0, int64_t end, bool b_mode, i
     magic[i] = UINT64_MAX / base[i];
     if ((int64_t) base[i] < mid_limit) nmid = (int) i + 1;
   }
-  DevBuf d_base, d_magic, d_c, d_m, d_l, d_q;
+  DevBuf& d_base = c.tmp[T_PS_BASE];
+  DevBuf& d_magic = c.tmp[T_PS_MAGIC];
+  DevBuf& d_c = c.tmp[T_PS_C];
+  DevBuf& d_m = c.tmp[T_PS_M];
+  DevBuf& d_l = c.tmp[T_PS_L];
+  DevBuf& d_q = c.tmp[T_PS_Q];
   d_base.alloc(std::max<size_t>(base.size(), 1) * 4);
   d_magic.alloc(std::max<size_t>(base.size(), 1) * 8);
   d_c.alloc((size_t) o.nseg * 8);
@@ -819,7 +825,8 @@ static std::vector<int64_t> pi_lookup(Ctx& c, const std::vector<uint64_t>& v, cu
   if (v.empty()) return r;
   for (uint64_t t : v)
     if ((int64_t) t < 0 || (int64_t) t > c.tab.pibig_limit) fail(PCG_EINTERNAL, "pi lookup beyond the PiTable");
-  DevBuf dv, dr;
+  DevBuf& dv = c.tmp[T_LK_V];
+  DevBuf& dr = c.tmp[T_LK_R];
   dv.alloc(v.size() * 8);
   dr.alloc(v.size() * 8);
   PCG_CUDA(cudaMemcpyAsync(dv.p, v.data(), v.size() * 8, cudaMemcpyHostToDevice, s));
@@ -907,7 +914,9 @@ static PiParts pi_gourdon(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s)
     const int64_t nC2 = std::max<int64_t>(0, P.bC21 - P.bC20);
     // C1 products: count q per b, then expand
     int64_t nQ = 0;
-    DevBuf qlo, qcnt, qoff;
+    DevBuf& qlo = c.tmp[T_AC_QLO];
+    DevBuf& qcnt = c.tmp[T_AC_QCNT];
+    DevBuf& qoff = c.tmp[T_AC_QOFF];
     std::vector<int64_t> hq;
     if (nC1 > 0) {
       qlo.alloc((size_t) nC1 * 8);
@@ -926,7 +935,7 @@ static PiParts pi_gourdon(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s)
     const int64_t nout = nA + nC1 + nQ + nC2;
     i128 sum = 0;
     if (nout > 0) {
-      DevBuf outs;
+      DevBuf& outs = c.tmp[T_AC_OUTS];
       outs.alloc((size_t) nout * sizeof(PairOuter));
       PairOuter* o = outs.as<PairOuter>();
       if (nA) k_outer_A<<<(unsigned) ((nA + 127) / 128), 128, 0, s>>>(P, o);
@@ -967,7 +976,7 @@ static PiParts pi_gourdon(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s)
     double t1 = fnow_ms();
     const int64_t size = wheel2310().to_index((uint64_t) z) + 1;
     const int grid = c.num_sms * 8;
-    DevBuf part;
+    DevBuf& part = c.tmp[T_PHI0_PART];
     part.alloc((size_t) grid * 16);
     PCG_CUDA(cudaMemsetAsync(part.p, 0, (size_t) grid * 16, s));
     PhiTab PT = phi_tab(c);
@@ -1108,7 +1117,7 @@ int64_t phi_any(Ctx& c, int64_t x, int64_t a, const Tuning& tune, cudaStream_t s
   if (a > x / 2) return 1;
   if (a <= 8) {
     ensure_phi_tiny(c, (int) a, s);
-    DevBuf o;
+    DevBuf& o = c.tmp[T_PHI_ONE];
     o.alloc(16);
     k_phi_one<<<1, 1, 0, s>>>((uint64_t) x, phi_tab(c), o.as<i128>());
     PCG_CUDA(cudaGetLastError());
@@ -1153,7 +1162,7 @@ int64_t phi_any(Ctx& c, int64_t x, int64_t a, const Tuning& tune, cudaStream_t s
     const int64_t i1 = host_pi(c.tab, (uint64_t) iroot((u128) x, 3));
     if (i1 > a) {
       const int64_t n = i1 - a;
-      DevBuf outs;
+      DevBuf& outs = c.tmp[T_PHI_OUTS];
       outs.alloc((size_t) n * sizeof(PairOuter));
       k_outer_P3<<<(unsigned) ((n + 127) / 128), 128, 0, s>>>((uint64_t) x, a, i1, c.tab.primes.as<uint32_t>(),
                                                               c.tab.pibig.as<uint64_t>(), outs.as<PairOuter>());
@@ -1174,7 +1183,7 @@ int64_t phi_any(Ctx& c, int64_t x, int64_t a, const Tuning& tune, cudaStream_t s
     const Tables& T = c.tab;
     const int64_t size = wheel2310().to_index((uint64_t) y) + 1;
     const int grid = c.num_sms * 8;
-    DevBuf part;
+    DevBuf& part = c.tmp[T_PHI0_PART];
     part.alloc((size_t) grid * 16);
     PCG_CUDA(cudaMemsetAsync(part.p, 0, (size_t) grid * 16, s));
     PhiTab PT = phi_tab(c);

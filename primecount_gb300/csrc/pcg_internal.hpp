@@ -114,7 +114,18 @@ void ensure_factor_d(Ctx& c, int64_t y, int64_t z, cudaStream_t s);
 void ensure_factor_dr(Ctx& c, int64_t y, cudaStream_t s);
 
 // device exclusive scan (uint32 -> uint64), synchronous on s
-void exclusive_scan_u32(const uint32_t* in, int64_t n, uint64_t* out, cudaStream_t s);
+void exclusive_scan_u32(const uint32_t* in, int64_t n, uint64_t* out, cudaStream_t s, DevBuf* sums = nullptr);
+
+// slots of Ctx::tmp
+enum TmpSlot {
+  T_PS_BASE, T_PS_MAGIC, T_PS_C, T_PS_M, T_PS_L, T_PS_Q,      // prime sieve (B, small pi)
+  T_LK_V, T_LK_R,                                             // PiTable lookups
+  T_AC_QLO, T_AC_QCNT, T_AC_QOFF, T_AC_OUTS,                  // A + C outers
+  T_PR_PIECES, T_PR_FIRST, T_PR_SPLIT, T_PR_PART, T_PR_SUMS,  // pair sums
+  T_PHI0_PART, T_PHI_ONE, T_PHI_OUTS,                         // Phi0, phi(x, a)
+  T_SW_SEG, T_SW_XP,                                          // sweep segment and x/p tables
+  T_COUNT
+};
 // PiTable {count, bits} over [0, limit] without the primes array
 void build_pitab_only(DevBuf& out, int64_t limit, cudaStream_t s);
 
@@ -169,6 +180,10 @@ struct Ctx {
   Tables tab;
   // scratch of the sweep (grown on demand)
   DevBuf cnt, smu, segsum, run, acc, misc, msum;
+  // per-call temporaries, one slot per use site, kept and grown across calls
+  // (no cudaMalloc / cudaFree per call: cudaFree synchronises the device and
+  // would serialise the contexts of a worker pool)
+  DevBuf tmp[24];
   pcg_stats last{};
   std::string last_error;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};

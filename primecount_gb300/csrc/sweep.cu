@@ -1252,10 +1252,11 @@ void ensure_prime_tables(Ctx& c, int64_t limit, cudaStream_t s)
   t.build_ms += now_ms() - t0;
 }
 
-void exclusive_scan_u32(const uint32_t* in, int64_t n, uint64_t* out, cudaStream_t s)
+void exclusive_scan_u32(const uint32_t* in, int64_t n, uint64_t* out, cudaStream_t s, DevBuf* sums_buf)
 {
   int64_t nblk = (n + SCAN_ITEMS - 1) / SCAN_ITEMS;
-  DevBuf sums;
+  DevBuf local;
+  DevBuf& sums = sums_buf ? *sums_buf : local;
   sums.alloc((size_t) std::max<int64_t>(nblk, 1) * 8);
   k_scan_sums<<<(unsigned) nblk, 512, 0, s>>>(in, n, sums.as<uint64_t>());
   k_scan_serial<<<1, 1024, 0, s>>>(sums.as<uint64_t>(), nblk);
@@ -1641,7 +1642,7 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   // segment table: small segments where leaves are dense, full ones elsewhere
   std::vector<int64_t> seglo = plan_segments(pb, c.tab, L, x_star, pi_sqrt, bglob, (int64_t) words * 240, grid);
   int64_t nseg = (int64_t) seglo.size() - 1;
-  DevBuf segbuf;
+  DevBuf& segbuf = c.tmp[T_SW_SEG];
   segbuf.alloc(seglo.size() * 8);
   PCG_CUDA(cudaMemcpyAsync(segbuf.p, seglo.data(), seglo.size() * 8, cudaMemcpyHostToDevice, s));
 
@@ -1666,7 +1667,7 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   c.msum.alloc((size_t) cols * 8);
   c.misc.alloc(4096);
   uint64_t* d_xp = nullptr;
-  DevBuf xpbuf;
+  DevBuf& xpbuf = c.tmp[T_SW_XP];
   xpbuf.alloc(xp.size() * 8);
   d_xp = xpbuf.as<uint64_t>();
   PCG_CUDA(cudaMemcpyAsync(d_xp, xp.data(), xp.size() * 8, cudaMemcpyHostToDevice, s));
