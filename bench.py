@@ -351,13 +351,13 @@ def main():
         from primecount_gb300 import serve as sv
         stream = sv.make_stream(20261203, 2000, args.serve_seconds)
         budget = args.serve_budget if args.serve_budget > 0 else None
-        r = sv.run_served(stream, workers=4, max_x=10 ** 20, drain_s=30, latency_budget=budget)
+        r = sv.run_served(stream, workers=8, max_x=10 ** 20, drain_s=30, latency_budget=budget)
         r.pop("results")
         plain = sv.run_plain(stream, drain_s=30, latency_budget=budget)
         serve = {"served": r, "plain": plain,
                  "config": {"rate": 2000, "seconds": args.serve_seconds, "seed": 20261203,
                             "pi_x": "10^U(8,20)", "phi_x": "10^U(8,16)", "requests": len(stream),
-                            "latency_budget_s": budget, "workers": 4}}
+                            "latency_budget_s": budget, "workers": 8}}
 
     if rank != 0:
         return

@@ -92,7 +92,7 @@ WorkerPool g_pool;
 
 int pool_size(const pcg_opts* opts, size_t n)
 {
-  int w = (opts && opts->threads > 0) ? opts->threads : 4;
+  int w = (opts && opts->threads > 0) ? opts->threads : 8;
   w = std::max(1, std::min(w, 16));
   return (int) std::min<size_t>((size_t) w, std::max<size_t>(n, 1));
 }

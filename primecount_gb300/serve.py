@@ -262,7 +262,7 @@ def main():
     ap.add_argument("--rate", type=float, default=2000)
     ap.add_argument("--seconds", type=float, default=60)
     ap.add_argument("--seed", type=int, default=20261203)
-    ap.add_argument("--workers", type=int, default=4)
+    ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--max-x", default="1e20")
     ap.add_argument("--pi-max-exp", type=float, default=20)
     ap.add_argument("--drain", type=float, default=30)
