@@ -1376,11 +1376,9 @@ void ensure_factor_dr(Ctx& c, int64_t y, cudaStream_t s)
 template <typename FT, int NT>
 static void set_sweep_attr(size_t smem)
 {
-  static size_t set = 0;
-  if (set < smem) {
-    PCG_CUDA(cudaFuncSetAttribute(k_sweep<FT, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
-    set = smem;
-  }
+  // per device and cheap: set on every call (worker threads and several
+  // devices share the function)
+  PCG_CUDA(cudaFuncSetAttribute(k_sweep<FT, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem));
 }
 
 template <typename FT, int NT>
