@@ -7,7 +7,8 @@ serves:
     python -m primecount_gb300 1e18 --S2-hard        S2_hard(x) with the default y, z, c
     python -m primecount_gb300 1e20 --AC | --B | --Phi0 | --Sigma
     python -m primecount_gb300 1e12 78498 --phi      phi(x, a)
-    options: -s / --status (print the parameters), --time, -t / --threads N
+    options: -s / --status (print the parameters), --time, -t / --threads N,
+             --alpha-y=A, --alpha-z=A (Gourdon's y = A x^(1/3), z = A y for pi(x))
 
 Numbers are integer expressions as the reference's calculator accepts them:
 1e20, 10^20, 2^64-1, 10**18 + 7 (integers only).  The result is printed on
@@ -57,6 +58,7 @@ OPTIONS = {"--D": "D", "-D": "D", "--S2-hard": "S2_hard", "--AC": "AC", "--B": "
 def main(argv=None):
     argv = sys.argv[1:] if argv is None else argv
     numbers, option, status, timing, threads = [], "pi", False, False, 0
+    alpha_y = alpha_z = 0.0
     i = 0
     while i < len(argv):
         a = argv[i]
@@ -71,6 +73,10 @@ def main(argv=None):
             threads = int(argv[i])
         elif a.startswith("--threads="):
             threads = int(a.split("=", 1)[1])
+        elif a.startswith("--alpha-y="):
+            alpha_y = float(a.split("=", 1)[1])
+        elif a.startswith("--alpha-z="):
+            alpha_z = float(a.split("=", 1)[1])
         elif a in ("-h", "--help"):
             print(__doc__)
             return 0
@@ -101,14 +107,14 @@ def main(argv=None):
         if status and x > 10 ** 10:
             p = pcg.gourdon_params(x)
             print("x = %d\ny = %d\nz = %d\nk = %d\nx_star = %d" % (x, p["y"], p["z"], p["k"], p["x_star"]))
-        r = pcg.pi(x, threads=threads)
+        r = pcg.pi(x, threads=threads, alpha_y=alpha_y, alpha_z=alpha_z)
     else:
         if x <= 10 ** 10:
             raise pcg.PrimecountError(1, "--%s: the formula terms are computed for x > 1e10" % option)
         if status:
             p = pcg.gourdon_params(x)
             print("x = %d\ny = %d\nz = %d\nk = %d\nx_star = %d" % (x, p["y"], p["z"], p["k"], p["x_star"]))
-        r = pcg.pi_terms(x)[option]
+        r = pcg.pi_terms(x, alpha_y=alpha_y, alpha_z=alpha_z)[option]
     dt = time.perf_counter() - t0
     if status:
         st = pcg.last_stats()

@@ -72,3 +72,14 @@ def test_phi_all_regimes_against_oracle(pcg, ora):
         x = int(10 ** rng.uniform(6, 9))
         a = rng.choice([rng.randint(1, 8), rng.randint(9, 40), rng.randint(40, 1200)])
         assert pcg.phi(x, a) == ora.phi(x, a), (x, a)
+
+
+@pytest.mark.gpu
+def test_pi_other_alpha(pcg, golden):
+    """pi(x) does not depend on Gourdon's y and z: other alpha_y / alpha_z (the
+    reference's --alpha-y / --alpha-z) give the same counts."""
+    for n in (12, 15, 18):
+        x = 10 ** n
+        want = golden["pi_pow10"][str(x)]
+        for ay, az in ((0, 2.0), (0, 3.5), (1.5, 1.0), (4.0, 1.5)):
+            assert pcg.pi(x, alpha_y=ay, alpha_z=az) == want, (x, ay, az)
