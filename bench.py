@@ -109,8 +109,9 @@ def cpu_baseline(p, threads, target_s=12.0):
     D(1e20): nchunks sub-intervals starting at c / nchunks of [0, x/z), all
     host threads.  The rate is the sample's leaves over its wall time (the
     metric's unit); the sample fraction grows until it takes about target_s
-    (at most 10x per step while it is tiny, 2x once it takes 0.3 s: its cost
-    grows faster than the fraction, the leaves being densest near 0)."""
+    (at most 10x per step while it is tiny; then by the 4th root of the
+    remaining factor: its cost grows much faster than the fraction, the
+    leaves being densest near 0)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.load()
@@ -119,7 +120,10 @@ def cpu_baseline(p, threads, target_s=12.0):
     leaves, secs = oracle.D_sample(X, p["y"], p["z"], p["k"], nchunks, frac, threads)
     spent = secs
     while secs < target_s * 2 / 3 and frac < 0.05:
-        step = min(10.0 if secs < 0.3 else 2.0, 0.8 * target_s / max(secs, 1e-3))
+        # the sample's cost grows about as its fraction to the 4th power once
+        # the first sub-interval reaches the dense start of the interval
+        step = min(10.0, 0.8 * target_s / max(secs, 1e-3)) if secs < 0.3 else \
+            max(1.1, min(2.0, (target_s / secs) ** 0.25))
         frac = min(0.05, frac * step)
         leaves, secs = oracle.D_sample(X, p["y"], p["z"], p["k"], nchunks, frac, threads)
         spent += secs
