@@ -83,3 +83,10 @@ def test_pi_other_alpha(pcg, golden):
         want = golden["pi_pow10"][str(x)]
         for ay, az in ((0, 2.0), (0, 3.5), (1.5, 1.0), (4.0, 1.5)):
             assert pcg.pi(x, alpha_y=ay, alpha_z=az) == want, (x, ay, az)
+
+
+def test_pi_1e20_and_1e21(pcg, golden):
+    # the 128-bit path end to end: x = 1e21 > 2^64 (README of the reference)
+    for n in (20, 21):
+        x = 10 ** n
+        assert pcg.pi(x) == golden["pi_pow10"][str(x)], n
