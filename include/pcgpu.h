@@ -171,6 +171,24 @@ pcg_status pcg_shard_combine(int nshards, int64_t cols, const pcg_i128* acc, con
 pcg_status pcg_D_noalloc(pcg_ctx* ctx, pcg_i128 x, int64_t y, int64_t z, int64_t k,
                          void* stream, pcg_i128* out);
 
+/* A sweep configuration: segment words, resident CTAs per SM, threads per
+ * CTA, levels per group (the b-range answered in one pass), and its time. */
+typedef struct {
+  int segment_words;
+  int ctas_per_sm;
+  int cta_threads;
+  int group;
+  double ms;
+} pcg_tuning;
+
+/* Autotuner (no counterpart in the reference, whose LoadBalancerS2 adapts
+ * chunk sizes at run time instead).  Times D(x) with the reference's default
+ * parameters under each candidate configuration on the context's device and
+ * keeps the fastest for x's decade in the context: later D / S2_hard / pi
+ * calls on that context whose tuning fields are 0 use it.  *best (may be
+ * NULL) receives the choice; the context must be opts->ctx (not NULL). */
+pcg_status pcg_autotune(pcg_i128 x, const pcg_opts* opts, pcg_tuning* best);
+
 /* D(x) / S2_hard(x) with the reference's default parameters
  * (the --D / --S2-hard command-line options, src/app/main.cpp:205-246,
  * 435-461).  y, z, k (c) are written when the pointers are non-NULL. */

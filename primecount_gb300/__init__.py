@@ -46,6 +46,11 @@ class Opts(ctypes.Structure):
                 ("stop_after_waves", ctypes.c_int)]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("segment_words", ctypes.c_int), ("ctas_per_sm", ctypes.c_int), ("cta_threads", ctypes.c_int),
+                ("group", ctypes.c_int), ("ms", ctypes.c_double)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("leaves", ctypes.c_uint64), ("two_prime_leaves", ctypes.c_uint64),
                 ("segments", ctypes.c_uint64), ("levels", ctypes.c_uint64),
@@ -116,6 +121,8 @@ def load(path=None):
     L.pcg_D_shard.argtypes = shard_args
     L.pcg_S2_hard_shard.argtypes = shard_args
     L.pcg_shard_combine.argtypes = [ctypes.c_int, c_i64, c_p(I128), c_p(c_i64), c_p(c_i64), c_p(I128)]
+    L.pcg_autotune.argtypes = [I128, c_p(Opts), c_p(Tuning)]
+    L.pcg_autotune.restype = ctypes.c_int
     for name in ("pcg_D", "pcg_S2_hard", "pcg_D_default", "pcg_S2_hard_default", "pcg_gourdon_params",
                  "pcg_dr_params", "pcg_pi", "pcg_phi", "pcg_pi_batch", "pcg_phi_batch", "pcg_ctx_create",
                  "pcg_last_stats", "pcg_D_shard", "pcg_S2_hard_shard", "pcg_shard_combine"):
@@ -332,3 +339,12 @@ def shard_combine(parts):
     out = I128()
     _check(load().pcg_shard_combine(n, cols, acc, ms, cs, ctypes.byref(out)))
     return from_i128(out)
+
+
+def autotune(x, ctx):
+    """Time the sweep configurations on D(x) and keep the fastest in ctx for
+    x's decade (pcg_autotune); returns the choice as a dict."""
+    t = Tuning()
+    o = _opts(ctx, None)
+    _check(load().pcg_autotune(to_i128(x), ctypes.byref(o), ctypes.byref(t)), ctx)
+    return {k: getattr(t, k) for k, _ in t._fields_}

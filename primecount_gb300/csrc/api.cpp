@@ -476,6 +476,64 @@ pcg_status pcg_S2_hard_shard(pcg_i128 x, int64_t y, int64_t z, int64_t c, int sh
   return hard_leaves_shard(false, x, y, z, c, shard, nshards, opts, acc, msum, csum, cap, cols);
 }
 
+pcg_status pcg_autotune(pcg_i128 xi, const pcg_opts* opts, pcg_tuning* best)
+{
+  if (!opts || !opts->ctx) return PCG_EINVAL;
+  Ctx* cp = nullptr;
+  return guard(nullptr, [&] {
+    cp = ctx_from(opts);
+    Ctx& c = *cp;
+    c.last_error.clear();
+    if (xi.hi < 0) fail(PCG_EINVAL, "x must be >= 0");
+    const u128 x = make_u128(xi);
+    if (x < 1000) fail(PCG_EINVAL, "autotune needs x >= 1000");
+    const GourdonParams g = gourdon_params(x);
+    check_hard_args(x, g.y, g.z, g.k, true);
+    const int e = (int) std::floor(std::log10((double) x));
+    c.tuned[e] = false;
+    cudaStream_t s = stream_from(c, opts);
+    // candidates: the measured defaults first, then their neighbours
+    static const int cand[][4] = {
+        {8192, 0, 256, 16}, {8192, 0, 256, 8}, {8192, 0, 256, 32}, {8192, 0, 256, 0},
+        {6144, 0, 256, 16}, {16384, 0, 512, 16}, {4096, 0, 128, 16}, {8192, 0, 128, 16}};
+    SweepProblem p;
+    p.gourdon = 1;
+    p.x = x;
+    p.y = g.y;
+    p.z = g.z;
+    p.k = g.k;
+    Tuning t0;
+    t0.group = 16;
+    t0.segment_words = 8192;
+    t0.cta_threads = 256;
+    run_sweep(c, p, t0, s);   // tables and scratch built outside the timed runs
+    Tuning bt;
+    double bms = 1e300;
+    i128 ref = 0;
+    bool have = false;
+    for (const auto& k : cand) {
+      Tuning t;
+      t.segment_words = k[0];
+      t.ctas_per_sm = k[1];
+      t.cta_threads = k[2];
+      t.group = k[3];
+      SweepResult r = run_sweep(c, p, t, s);
+      if (!have) { ref = r.sum; have = true; }
+      else if (r.sum != ref) fail(PCG_EINTERNAL, "autotune: configurations disagree");
+      if (r.stats.sweep_ms < bms) { bms = r.stats.sweep_ms; bt = t; }
+    }
+    c.tuned_cfg[e] = bt;
+    c.tuned[e] = true;
+    if (best) {
+      best->segment_words = bt.segment_words;
+      best->ctas_per_sm = bt.ctas_per_sm;
+      best->cta_threads = bt.cta_threads;
+      best->group = bt.group;
+      best->ms = bms;
+    }
+  });
+}
+
 pcg_status pcg_shard_combine(int nshards, int64_t cols, const pcg_i128* acc, const int64_t* msum,
                              const int64_t* csum, pcg_i128* out)
 {

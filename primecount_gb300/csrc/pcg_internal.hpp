@@ -151,6 +151,7 @@ struct Tuning {
   std::string checkpoint;            // sweep checkpoint file ("" = none)
   double checkpoint_interval = 0;    // seconds between checkpoint writes
   int stop_after_waves = 0;          // > 0: stop (checkpointed) after this many waves
+  int group = -1;                    // levels per group in the sweep (-1: default)
 };
 
 struct SweepResult {
@@ -184,6 +185,9 @@ struct Ctx {
   // (no cudaMalloc / cudaFree per call: cudaFree synchronises the device and
   // would serialise the contexts of a worker pool)
   DevBuf tmp[24];
+  // sweep configurations chosen by pcg_autotune, by decimal exponent of x
+  bool tuned[64] = {};
+  Tuning tuned_cfg[64];
   pcg_stats last{};
   std::string last_error;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};

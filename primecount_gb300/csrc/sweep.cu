@@ -32,6 +32,7 @@
 #include <chrono>
 #include <algorithm>
 #include <mutex>
+#include <cmath>
 #include <string>
 
 #include "pcg_internal.hpp"
@@ -1560,7 +1561,7 @@ static void write_checkpoint(const std::string& path, const CkptHeader& h, const
   if (!ok || rename(tmp.c_str(), path.c_str()) != 0) fail(PCG_EINVAL, "cannot write the checkpoint " + path);
 }
 
-SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaStream_t s)
+SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune_in, cudaStream_t s)
 {
   SweepResult res;
   pcg_stats& st = res.stats;
@@ -1616,7 +1617,19 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   }
 
   // tuning: threads per CTA, bitmap words per CTA, leaf-record capacity,
-  // resident CTAs per SM
+  // resident CTAs per SM; a configuration chosen by pcg_autotune for this
+  // decade of x replaces the defaults the caller left at 0
+  Tuning tune = tune_in;
+  {
+    const int e = (int) std::floor(std::log10((double) x));
+    if (e >= 0 && e < 64 && c.tuned[e] && !tune.segment_words && !tune.cta_threads && !tune.ctas_per_sm &&
+        tune.group < 0) {
+      tune.segment_words = c.tuned_cfg[e].segment_words;
+      tune.cta_threads = c.tuned_cfg[e].cta_threads;
+      tune.ctas_per_sm = c.tuned_cfg[e].ctas_per_sm;
+      tune.group = c.tuned_cfg[e].group;
+    }
+  }
   const int NT = (tune.cta_threads == 512 || tune.cta_threads == 128) ? tune.cta_threads : 256;
   int words = tune.segment_words > 0 ? tune.segment_words : 8192;
   const int wq = std::max(8 * NT, 2048);   // whole chunks per thread and per scan lane pair
@@ -1698,7 +1711,7 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune, cudaSt
   a.factor = pb.gourdon ? c.tab.factor_d.p : c.tab.factor_dr.p;
   a.xp_tab = d_xp;
   a.coprime = c.tab.coprime.as<uint16_t>();
-  a.group_max = sweep_group_max();
+  a.group_max = tune.group >= 0 ? std::min(tune.group, GROUP_MAX) : sweep_group_max();
   a.cindex = c.tab.cindex.as<int16_t>();
   a.finv = c.tab.finv.as<uint64_t>();
   a.pmagic = c.tab.pmagic.as<uint64_t>();
