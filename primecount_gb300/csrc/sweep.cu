@@ -463,6 +463,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
   __shared__ int s_ws;
   __shared__ uint32_t wtmp[32];
   __shared__ int s_gsmu[GROUP_MAX];                    // signed leaf counts of a level group
+  __shared__ uint64_t s_gmag[GROUP_MAX];               // reciprocals of the group's primes
   __shared__ int s_smu;
   __shared__ int s_stop;
   __shared__ uint32_t s_rem[3];
@@ -887,7 +888,10 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
             while (lj < nb && lj - li < A.group_max && (lp[lj].flags & 8) && loff[lj + 1] <= wend) lj++;
             if (lj - li >= 2) {
               const int ra = (int) (loff[li] - w0), rb = (int) (loff[lj] - w0);
-              if (tid < lj - li) s_gsmu[tid] = 0;
+              if (tid < lj - li) {
+                s_gsmu[tid] = 0;
+                s_gmag[tid] = A.pmagic[b0 + li + tid];
+              }
               if (rb > ra && dirty) { scan_chunks(ccount, pref, nch, wtmp); dirty = false; }
               else __syncthreads();
               if (rb > ra) {
@@ -904,7 +908,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                     for (int b = li; b < lv; b++) {
                       const uint64_t pb = lp[b].prime;
                       if (pb <= n && pb >= (uint64_t) low) c--;
-                      const int64_t d = dpi(A.pitab, div_magic(n, pb, A.pmagic[b0 + b])) - (int64_t) s_pc[b];
+                      const int64_t d = dpi(A.pitab, div_magic(n, pb, s_gmag[b - li])) - (int64_t) s_pc[b];
                       if (d > 0) c -= (uint32_t) d;
                     }
                     if (r & (1u << 30)) { lsum -= c; sg = -1; }
