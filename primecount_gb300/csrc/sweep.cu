@@ -905,7 +905,28 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                     const uint32_t off = r & 0x3FFFFFFFu;
                     uint32_t c = query(bits, pref, off);
                     const uint64_t n = (uint64_t) low + off;
-                    for (int b = li; b < lv; b++) {
+                    // four levels at a time: their PiTable words are loaded together
+                    int b = li;
+                    for (; b + 4 <= lv; b += 4) {
+                      uint64_t t[4];
+#pragma unroll
+                      for (int u = 0; u < 4; u++) {
+                        const uint64_t pb = lp[b + u].prime;
+                        if (pb <= n && pb >= (uint64_t) low) c--;
+                        t[u] = div_magic(n, pb, s_gmag[b + u - li]);
+                      }
+                      ulonglong2 e[4];
+#pragma unroll
+                      for (int u = 0; u < 4; u++) e[u] = ((const ulonglong2*) A.pitab)[t[u] / 240];
+#pragma unroll
+                      for (int u = 0; u < 4; u++) {
+                        // for t < 6 this reads 3 + a few bits, still below s_pc[b] >= pi(63): dropped by d > 0
+                        const int64_t pt = (int64_t) (e[u].x + __popcll(e[u].y & mask_le((uint32_t) (t[u] % 240))));
+                        const int64_t d = pt - (int64_t) s_pc[b + u];
+                        if (d > 0) c -= (uint32_t) d;
+                      }
+                    }
+                    for (; b < lv; b++) {
                       const uint64_t pb = lp[b].prime;
                       if (pb <= n && pb >= (uint64_t) low) c--;
                       const int64_t d = dpi(A.pitab, div_magic(n, pb, s_gmag[b - li])) - (int64_t) s_pc[b];
