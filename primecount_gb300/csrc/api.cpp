@@ -494,8 +494,8 @@ pcg_status pcg_autotune(pcg_i128 xi, const pcg_opts* opts, pcg_tuning* best)
     cudaStream_t s = stream_from(c, opts);
     // candidates: the measured defaults first, then their neighbours
     static const int cand[][4] = {
-        {8192, 0, 256, 16}, {8192, 0, 256, 8}, {8192, 0, 256, 32}, {8192, 0, 256, 0},
-        {6144, 0, 256, 16}, {16384, 0, 512, 16}, {4096, 0, 128, 16}, {8192, 0, 128, 16}};
+        {8192, 0, 256, 32}, {8192, 0, 256, 16}, {8192, 0, 256, 64}, {8192, 0, 256, 0},
+        {6144, 0, 256, 32}, {16384, 0, 512, 32}, {4096, 0, 128, 32}, {8192, 0, 128, 32}};
     SweepProblem p;
     p.gourdon = 1;
     p.x = x;
@@ -503,7 +503,7 @@ pcg_status pcg_autotune(pcg_i128 xi, const pcg_opts* opts, pcg_tuning* best)
     p.z = g.z;
     p.k = g.k;
     Tuning t0;
-    t0.group = 16;
+    t0.group = 32;
     t0.segment_words = 8192;
     t0.cta_threads = 256;
     run_sweep(c, p, t0, s);   // tables and scratch built outside the timed runs

@@ -1515,7 +1515,7 @@ static int sweep_group_max()
 {
   static const int g = [] {
     const char* e = getenv("PCG_SWEEP_GROUP");
-    const int v = e ? atoi(e) : 16;
+    const int v = e ? atoi(e) : 32;
     return v < 0 ? 0 : (v > GROUP_MAX ? GROUP_MAX : v);
   }();
   return g;
