@@ -63,7 +63,7 @@ typedef struct pcg_ctx pcg_ctx;
 typedef struct {
   pcg_ctx* ctx;          /* NULL: the library's default context of the current device */
   void* stream;          /* cudaStream_t to launch on; NULL: the context's stream      */
-  int threads;           /* host threads (reference `threads`); 0 = all                */
+  int threads;           /* batches: worker contexts on the GPU (0 = 8); else unused   */
   int print;             /* reference is_print: print variables and timings            */
   int segment_words;     /* sieve segment in 64-bit words (x240 numbers); 0 = autotune */
   int ctas_per_sm;       /* resident CTAs per SM for the sweep; 0 = autotune           */
