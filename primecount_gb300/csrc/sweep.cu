@@ -413,6 +413,16 @@ __device__ __forceinline__ uint32_t query(const uint64_t* __restrict__ bits, con
          part(5, w45.y) + part(6, w67.x) + part(7, w67.y);
 }
 
+// Cross off the number at offset w * 240 + rr of the segment: a 32-bit atomic
+// on the half of the 64-bit word that holds its bit (bits 0-31 of a word are
+// the lower half), true when the number was still unsieved
+__device__ __forceinline__ bool cross_off(uint64_t* bits, uint32_t w, uint32_t rr)
+{
+  const uint32_t bi = bit_of(rr);
+  const uint32_t m = 1u << (bi & 31);
+  return (atomicAnd((uint32_t*) bits + 2 * w + (bi >> 5), ~m) & m) != 0;
+}
+
 // Record of one table entry: the offset of the leaf in the segment, bit 30 =
 // negative sign, or REC_NONE when the factor-table filter rejects the entry.
 #define REC_NONE 0xFFFFFFFFu
@@ -865,9 +875,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
               const uint64_t q = 30 * (jj >> 3) + woff((uint32_t) (jj & 7));
               const uint32_t off = (uint32_t) ((uint64_t) Q.prime * q - (uint64_t) low);
               const uint32_t w = off / 240, rr = off - w * 240;
-              const uint64_t m = 1ull << bit_of(rr);
-              const uint64_t old = atomicAnd((unsigned long long*) &bits[w], ~m);
-              if (old & m) atomicSub(&ccount[w >> 3], 1u);
+              if (cross_off(bits, w, rr)) atomicSub(&ccount[w >> 3], 1u);
             }
             const uint32_t removed = (uint32_t) (rpre[re] - r0);
             total -= removed;
@@ -963,9 +971,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                 const uint64_t q = 30 * (jj >> 3) + woff((uint32_t) (jj & 7));
                 const uint32_t off = (uint32_t) ((uint64_t) Q.prime * q - (uint64_t) low);
                 const uint32_t w = off / 240, rr = off - w * 240;
-                const uint64_t m = 1ull << bit_of(rr);
-                const uint64_t old = atomicAnd((unsigned long long*) &bits[w], ~m);
-                if (old & m) atomicSub(&ccount[w >> 3], 1u);
+                if (cross_off(bits, w, rr)) atomicSub(&ccount[w >> 3], 1u);
               }
               total -= (uint32_t) (rpre[lj] - r0);
               if (h1 > h0) dirty = true;
@@ -1032,12 +1038,14 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
               const uint64_t jj = P.jlo + (uint64_t) tid;
               const uint64_t q = 30 * (jj >> 3) + woff((uint32_t) (jj & 7));
               const uint32_t off = (uint32_t) (p * q - (uint64_t) low);
-              uint32_t w = off / 240;
-              const uint64_t m = 1ull << bit_of(off - w * 240);
-              const uint32_t wstep = (uint32_t) p * (NT / 64);
-              for (uint32_t j = tid; j < P.jn; j += NT, w += wstep) {
-                const uint64_t old = atomicAnd((unsigned long long*) &bits[w], ~m);
-                if (old & m) { rem++; atomicSub(&ccount[w >> 3], 1u); }
+              const uint32_t w = off / 240;
+              const uint32_t bi = bit_of(off - w * 240);
+              const uint32_t m = 1u << (bi & 31);
+              // the number's 32-bit half-word, and the half-word stride
+              uint32_t h = 2 * w + (bi >> 5);
+              const uint32_t hstep = (uint32_t) p * (NT / 32);
+              for (uint32_t j = tid; j < P.jn; j += NT, h += hstep) {
+                if (atomicAnd((uint32_t*) bits + h, ~m) & m) { rem++; atomicSub(&ccount[h >> 4], 1u); }
               }
             }
           }
