@@ -475,6 +475,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
   __shared__ int s_gsmu[GROUP_MAX];                    // signed leaf counts of a level group
   __shared__ uint64_t s_gmag[GROUP_MAX];               // reciprocals of the group's primes
   __shared__ int s_smu;
+  __shared__ int s_ncomp[2];                           // accepted records of a compacted window, by window parity
   __shared__ int s_stop;
   __shared__ uint32_t s_rem[3];
   __shared__ uint32_t s_total;
@@ -545,7 +546,10 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
       if (w == wused - 1) v &= mask_le((span - 1) % 240);
       bits[w] = v;
     }
-    if (tid == 0) { s_total = 0; s_rem[0] = s_rem[1] = s_rem[2] = 0; s_smu = 0; s_stop = 0x7FFFFFFF; }
+    if (tid == 0) {
+      s_total = 0; s_rem[0] = s_rem[1] = s_rem[2] = 0; s_smu = 0; s_stop = 0x7FFFFFFF;
+      s_ncomp[0] = s_ncomp[1] = 0;
+    }
     __syncthreads();
     {
       uint32_t part = 0;
@@ -563,6 +567,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
     bool dirty = true;
     long long lsum = 0;
     unsigned long long nleaves = 0, ntwo = 0, nentries = 0;
+    unsigned win = 0;      // windows of the segment so far (parity selects the compaction counter)
 
     for (int b0 = 1; b0 <= Bs; b0 += NT) {
       // ---- per-level parameters of levels b0 .. b0+NT-1, one thread each
@@ -690,6 +695,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
       int64_t w0 = 0;      // first flat record of the window
       while (li < nb) {
         const int64_t wend = w0 + cap;
+        win++;
         // ---- phase A: the window's leaf records, flat over levels, PA_UNROLL
         // entries per thread in three stages so that their table loads, then
         // their reciprocal loads, are in flight together
@@ -697,6 +703,13 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
         // a window inside one level (the dense case): that level's constants
         // held in registers, no level lookup per entry
         const bool one_level = nrec > 0 && loff[li] <= w0 && loff[li + 1] >= w0 + nrec;
+        // a window of one level of FactorTable entries whose records are all
+        // answered by the per-level path: the accepted records are compacted
+        // to the front (their order is free, all are answered against one
+        // bitmap state), the rejected ones are dropped
+        const bool compact = one_level && !(lp[li].flags & 2) && (loff[li] < w0 || !(lp[li].flags & 8));
+        const int clev = compact ? li : -1;                // the level whose records are compacted
+        if (tid == 0) s_ncomp[(win + 1) & 1] = 0;
         if (one_level) {
           const LevelP& Q = lp[li];
           const int64_t hi0 = Q.hi - (w0 - loff[li]);        // table index of entry f is hi0 - f
@@ -705,7 +718,8 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
           const uint64_t* xt = A.xp_tab + 3 * (int64_t) Q.level;
           const uint64_t xlo = xt[0], xhi = xt[1];
           unsigned nl = 0;
-          for (int f0 = tid; f0 < nrec; f0 += PA_UNROLL * NT) {
+          // f0 - lane is the same for the lanes of a warp: the loop is warp-uniform
+          for (int f0 = tid; f0 - lane < nrec; f0 += PA_UNROLL * NT) {
             uint32_t fv[PA_UNROLL];
             uint64_t minv[PA_UNROLL];
 #pragma unroll
@@ -724,9 +738,11 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                 }
               }
             }
+            uint32_t rv[PA_UNROLL];
 #pragma unroll
             for (int u = 0; u < PA_UNROLL; u++) {
               const int f = f0 + u * NT;
+              rv[u] = REC_NONE;
               if (f < nrec) {
                 const int64_t idx = hi0 - f;
                 uint64_t m = 0;
@@ -739,14 +755,33 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                     m = 2310ull * ((uint64_t) idx / 480) + cop[(uint64_t) idx % 480];
                   }
                 }
-                uint32_t r = REC_NONE;
                 if (m) {
                   const uint64_t nn = xhi == 0 ? div_magic(xlo, m, minv[u]) : div_xp(xlo, xhi, m);
-                  r = (uint32_t) (nn - (uint64_t) low);
+                  uint32_t r = (uint32_t) (nn - (uint64_t) low);
                   if (!two && !(fv[u] & 1)) r |= 1u << 30;
+                  rv[u] = r;
                   nl++;
                 }
-                rec[f] = r;
+                if (!compact) rec[f] = rv[u];
+              }
+            }
+            if (compact) {
+              // one shared counter update per warp for its PA_UNROLL x 32 entries
+              unsigned bal[PA_UNROLL];
+              int tot = 0;
+#pragma unroll
+              for (int u = 0; u < PA_UNROLL; u++) {
+                bal[u] = __ballot_sync(0xffffffffu, rv[u] != REC_NONE);
+                tot += __popc(bal[u]);
+              }
+              int base = 0;
+              if (lane == 0 && tot) base = atomicAdd(&s_ncomp[win & 1], tot);
+              base = __shfl_sync(0xffffffffu, base, 0);
+              const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+              for (int u = 0; u < PA_UNROLL; u++) {
+                if (rv[u] != REC_NONE) rec[base + __popc(bal[u] & lt)] = rv[u];
+                base += __popc(bal[u]);
               }
             }
           }
@@ -984,7 +1019,9 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
           if (lz > la && la >= wend) break;               // records start in a later window
           const int l = b0 + li;
           if (la >= w0 && tid == 0) A.cnt[(int64_t) ws * cols + l] = total;
-          const int ra = (int) (dmax(la, w0) - w0), rb = (int) (dmin(lz, wend) - w0);
+          const int ra = (int) (dmax(la, w0) - w0);
+          const int rz = (int) (dmin(lz, wend) - w0);           // end of the level's window records
+          const int rb = li == clev ? s_ncomp[win & 1] : rz;   // end of those still to answer
           if (rb > ra) {
             if (dirty) { scan_chunks(ccount, pref, nch, wtmp); dirty = false; }
             if (ra + 32 * warp < rb) {
@@ -1001,8 +1038,8 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
               if (lane == 0 && smu_t) atomicAdd(&s_smu, smu_t);
             }
             __syncthreads();
-            if (lz <= wend && tid == 0) { A.smu[(int64_t) ws * cols + l] = s_smu; s_smu = 0; }
           }
+          if (rz > ra && lz <= wend && tid == 0) { A.smu[(int64_t) ws * cols + l] = s_smu; s_smu = 0; }
           if (lz > wend) break;                            // the level continues in the next window
           // ---- cross off p_l and its multiples, count the numbers removed first
           const LevelP& P = lp[li];
