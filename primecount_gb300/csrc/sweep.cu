@@ -293,12 +293,16 @@ __global__ void k_factor_zero_small(T* __restrict__ out, int64_t size, int64_t l
 
 // ================================================================ the sweep
 struct LevelP {
-  int64_t lo, hi;     // leaf range (lo, hi]: factor indices (family 1) or prime indices (family 2)
+  union {
+    int64_t lo;       // leaf range (lo, hi] while the levels are set up ...
+    uint64_t xlo;     // ... then the low word of x / p (flag 16: the high word is not 0)
+  };
+  int64_t hi;         // factor indices (family 1) or prime indices (family 2)
   uint64_t jlo;       // first 30-coprime rank of the cross-off co-factors
   uint32_t jn;        // number of cross-off co-factors
   uint32_t prime;
   uint32_t thr;       // factor-table threshold (family 1)
-  uint32_t flags;     // 1: leaves, 2: family 2, 4: small prime (pattern cross-off), 8: formula count
+  uint32_t flags;     // 1: leaves, 2: family 2, 4: small prime (pattern cross-off), 8: formula count, 16: x / p >= 2^64
   int32_t level;      // b
   uint32_t fcount;    // flag 8: numbers of the segment removed at this level (PiTable formula)
 };
@@ -657,7 +661,11 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
               }
             }
             if (stop) atomicMin(&s_stop, b);
-            if (P.flags & 1) E = P.hi - P.lo;
+            if (P.flags & 1) {
+              E = P.hi - P.lo;
+              P.xlo = xt[0];
+              if (xt[1]) P.flags |= 16;
+            }
           }
         }
         fcnt = P.fcount;
@@ -789,35 +797,41 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
           if (two) ntwo += nl;
         }
         if (nrec > 0 && !one_level) {
-          int lv = li;       // level of this thread's previous entry
+          // the window's records belong to levels li .. lw
+          int lw = li;
+          {
+            const int64_t last = w0 + nrec - 1;
+            int hi = nb - 1;
+            while (lw < hi) {
+              const int mid = (lw + hi + 1) >> 1;
+              if (loff[mid] <= last) lw = mid; else hi = mid - 1;
+            }
+          }
           for (int f0 = tid; f0 < nrec; f0 += PA_UNROLL * NT) {
             int jl[PA_UNROLL];
             int el[PA_UNROLL];
             uint32_t fv[PA_UNROLL];
+            // the level of each entry, the last with loff <= its position: a
+            // branch-free binary search over li .. lw, the entries' searches
+            // interleaved so that their shared-memory loads overlap
+#pragma unroll
+            for (int u = 0; u < PA_UNROLL; u++) jl[u] = li;
+            for (int n = lw - li + 1; n > 1;) {
+              const int half = n >> 1;
+#pragma unroll
+              for (int u = 0; u < PA_UNROLL; u++) {
+                const int64_t pos = w0 + min(f0 + u * NT, nrec - 1);
+                const int c = jl[u] + half;
+                jl[u] = loff[c] <= pos ? c : jl[u];
+              }
+              n -= half;
+            }
 #pragma unroll
             for (int u = 0; u < PA_UNROLL; u++) {
               const int f = f0 + u * NT;
-              jl[u] = -1;
-              el[u] = 0;
+              el[u] = (int) (w0 + f - loff[jl[u]]);
               fv[u] = 0;
-              if (f < nrec) {
-                const int64_t pos = w0 + f;
-                // last level with loff <= pos: a few steps forward from the
-                // previous entry's level, else a binary search
-                int lo = lv;
-                int steps = 0;
-                while (lo + 1 < nb && loff[lo + 1] <= pos && steps < 4) { lo++; steps++; }
-                if (lo + 1 < nb && loff[lo + 1] <= pos) {
-                  int hi = nb - 1;
-                  while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (loff[mid] <= pos) lo = mid; else hi = mid - 1;
-                  }
-                }
-                lv = lo;
-                jl[u] = lo;
-                el[u] = (int) (pos - loff[lo]);
-              }
+              if (f >= nrec) jl[u] = -1;
             }
             // table entries and the reciprocals of their divisors, loaded
             // together (the reciprocal of a rejected entry goes unused)
@@ -866,9 +880,8 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                 const LevelP& Q = lp[jl[u]];
                 uint32_t r = REC_NONE;
                 if (mdiv[u]) {
-                  const uint64_t* xt = A.xp_tab + 3 * (int64_t) Q.level;
-                  const uint64_t xlo = xt[0], xhi = xt[1];
-                  const uint64_t nn = xhi == 0 ? div_magic(xlo, mdiv[u], minv[u]) : div_xp(xlo, xhi, mdiv[u]);
+                  const uint64_t nn = (Q.flags & 16) ? div_xp(Q.xlo, A.xp_tab[3 * (int64_t) Q.level + 1], mdiv[u])
+                                                     : div_magic(Q.xlo, mdiv[u], minv[u]);
                   r = (uint32_t) (nn - (uint64_t) low);
                   if (!(Q.flags & 2) && !(fv[u] & 1)) r |= 1u << 30;
                   nleaves++;
