@@ -1140,37 +1140,60 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
   if (tid < 4 && s_ctr[tid]) atomicAdd(&A.counters[tid], s_ctr[tid]);
 }
 
-// ---- phi offsets: acc[b] += sum_s M(s, b) * sum_{s'<s} C(s', b), in segment order
-__global__ void k_combine(const uint32_t* __restrict__ cnt, const int32_t* __restrict__ smu,
-                          int wave_len, int cols, int64_t* __restrict__ run, i128* __restrict__ acc,
-                          int64_t* __restrict__ msum)
+// ---- phi offsets: acc[b] += sum_s M(s, b) * sum_{s'<s} C(s', b), in segment order.
+// A block takes 32 levels; its CW warps take consecutive runs of the wave's
+// segments and sum them from a local count of 0, then the runs are chained:
+// a run k whose segments see the count R_k + r (r its local prefix) adds
+// a_k + ms_k R_k, with a_k = sum M r and ms_k = sum M over the run.
+#define COMBINE_WARPS 16
+__global__ void __launch_bounds__(32 * COMBINE_WARPS)
+k_combine(const uint32_t* __restrict__ cnt, const int32_t* __restrict__ smu, int wave_len, int cols,
+          int64_t* __restrict__ run, i128* __restrict__ acc, int64_t* __restrict__ msum)
 {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= cols) return;
-  int64_t r = run[b];
+  __shared__ i128 s_a[COMBINE_WARPS][32];
+  __shared__ long long s_m[COMBINE_WARPS][32], s_c[COMBINE_WARPS][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int b = blockIdx.x * 32 + lane;
+  const int per = (wave_len + COMBINE_WARPS - 1) / COMBINE_WARPS;
+  const int s0 = min(wave_len, w * per), s1 = min(wave_len, s0 + per);
   i128 a = 0;
-  int64_t ms = 0;
-  int s = 0;
-  for (; s + 4 <= wave_len; s += 4) {
-    int32_t m0 = smu[(int64_t) s * cols + b], m1 = smu[(int64_t) (s + 1) * cols + b];
-    int32_t m2 = smu[(int64_t) (s + 2) * cols + b], m3 = smu[(int64_t) (s + 3) * cols + b];
-    uint32_t c0 = cnt[(int64_t) s * cols + b], c1 = cnt[(int64_t) (s + 1) * cols + b];
-    uint32_t c2 = cnt[(int64_t) (s + 2) * cols + b], c3 = cnt[(int64_t) (s + 3) * cols + b];
-    a += (i128) m0 * r; r += c0;
-    a += (i128) m1 * r; r += c1;
-    a += (i128) m2 * r; r += c2;
-    a += (i128) m3 * r; r += c3;
-    ms += (int64_t) m0 + m1 + m2 + m3;
+  long long ms = 0, r = 0;
+  if (b < cols) {
+    int s = s0;
+    for (; s + 4 <= s1; s += 4) {
+      const int32_t m0 = smu[(int64_t) s * cols + b], m1 = smu[(int64_t) (s + 1) * cols + b];
+      const int32_t m2 = smu[(int64_t) (s + 2) * cols + b], m3 = smu[(int64_t) (s + 3) * cols + b];
+      const uint32_t c0 = cnt[(int64_t) s * cols + b], c1 = cnt[(int64_t) (s + 1) * cols + b];
+      const uint32_t c2 = cnt[(int64_t) (s + 2) * cols + b], c3 = cnt[(int64_t) (s + 3) * cols + b];
+      a += (i128) m0 * r; r += c0;
+      a += (i128) m1 * r; r += c1;
+      a += (i128) m2 * r; r += c2;
+      a += (i128) m3 * r; r += c3;
+      ms += (long long) m0 + m1 + m2 + m3;
+    }
+    for (; s < s1; s++) {
+      const int32_t m = smu[(int64_t) s * cols + b];
+      a += (i128) m * r;
+      ms += m;
+      r += cnt[(int64_t) s * cols + b];
+    }
   }
-  for (; s < wave_len; s++) {
-    const int32_t m = smu[(int64_t) s * cols + b];
-    a += (i128) m * r;
-    ms += m;
-    r += cnt[(int64_t) s * cols + b];
+  s_a[w][lane] = a;
+  s_m[w][lane] = ms;
+  s_c[w][lane] = r;
+  __syncthreads();
+  if (w == 0 && b < cols) {
+    long long R = run[b], M = 0;
+    i128 A = 0;
+    for (int k = 0; k < COMBINE_WARPS; k++) {
+      A += s_a[k][lane] + (i128) s_m[k][lane] * R;
+      R += s_c[k][lane];
+      M += s_m[k][lane];
+    }
+    run[b] = R;
+    acc[b] += A;
+    if (msum) msum[b] += M;
   }
-  run[b] = r;
-  acc[b] += a;
-  if (msum) msum[b] += ms;
 }
 
 // ---- local leaf sums of a wave into acc[0] (column 0 is never a level)
@@ -1876,8 +1899,8 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune_in, cud
     else { if (fbytes == 2) launch_sweep<uint16_t, 128>(a, g, smem, s); else launch_sweep<uint32_t, 128>(a, g, smem, s); }
     PCG_CUDA(cudaGetLastError());
     PCG_CUDA(cudaEventRecord(c.kev[2 * waves + 1], s));
-    k_combine<<<(cols + 255) / 256, 256, 0, s>>>(a.cnt, a.smu, wl, cols, c.run.as<int64_t>(), c.acc.as<i128>(),
-                                                 c.msum.as<int64_t>());
+    k_combine<<<(cols + 31) / 32, 32 * COMBINE_WARPS, 0, s>>>(a.cnt, a.smu, wl, cols, c.run.as<int64_t>(),
+                                                             c.acc.as<i128>(), c.msum.as<int64_t>());
     k_segsum<<<1, 1024, 0, s>>>(a.segsum, wl, c.acc.as<i128>());
     PCG_CUDA(cudaGetLastError());
     launches += 3;
@@ -2190,7 +2213,7 @@ SweepResult run_sweep_noalloc(Ctx& c, const SweepProblem& pb, cudaStream_t s)
     if (fbytes == 2) launch_sweep<uint16_t, 256>(a, g, smem, s);
     else launch_sweep<uint32_t, 256>(a, g, smem, s);
     PCG_CUDA(cudaGetLastError());
-    k_combine<<<(cols + 255) / 256, 256, 0, s>>>(d_cnt, d_smu, wl, cols, d_run, d_acc, nullptr);
+    k_combine<<<(cols + 31) / 32, 32 * COMBINE_WARPS, 0, s>>>(d_cnt, d_smu, wl, cols, d_run, d_acc, nullptr);
     k_segsum<<<1, 1024, 0, s>>>(d_segsum, wl, d_acc);
     PCG_CUDA(cudaGetLastError());
     launches += 3;
