@@ -192,6 +192,8 @@ struct Ctx {
   std::string last_error;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::vector<cudaEvent_t> kev;   // per-launch timing events of the sweep
+  // the last segment plan of the sweep and the problem and launch shape it was made for
+  std::vector<int64_t> plan, plan_key;
   ~Ctx();
 };
 

@@ -34,6 +34,7 @@
 #include <mutex>
 #include <cmath>
 #include <string>
+#include <thread>
 
 #include "pcg_internal.hpp"
 #include "dev_common.cuh"
@@ -1551,12 +1552,23 @@ static std::vector<int64_t> plan_segments(const SweepProblem& pb, const Tables& 
     return (double) host_pi(t, (uint64_t) std::min(lim, (double) t.prime_limit));
   };
   const double c_level = 30.0;
-  std::vector<double> cum(g.size(), 0.0);
-  for (size_t i = 0; i + 1 < g.size(); i++) {
-    double len = g[i + 1] - g[i];
-    double c = len > 0 ? leaves(g[i], g[i + 1]) + c_level * levels(g[i]) * len / (double) smax : 0;
-    cum[i + 1] = cum[i] + c;
+  // the cost of each grid cell, the cells spread over the host threads
+  const size_t ncell = g.size() - 1;
+  std::vector<double> cost(ncell, 0.0);
+  {
+    const unsigned nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> th;
+    for (unsigned k = 0; k < nth; k++)
+      th.emplace_back([&, k] {
+        for (size_t i = k; i < ncell; i += nth) {
+          const double len = g[i + 1] - g[i];
+          cost[i] = len > 0 ? leaves(g[i], g[i + 1]) + c_level * levels(g[i]) * len / (double) smax : 0;
+        }
+      });
+    for (auto& t : th) t.join();
   }
+  std::vector<double> cum(g.size(), 0.0);
+  for (size_t i = 0; i < ncell; i++) cum[i + 1] = cum[i] + cost[i];
   const double total = cum.back();
   const double target = std::max(total / (grid * 6.0), 1.0);
   // cumulative cost at n (linear inside a grid cell)
@@ -1567,24 +1579,24 @@ static std::vector<int64_t> plan_segments(const SweepProblem& pb, const Tables& 
     double f = (g[i] > g[i - 1]) ? (n - g[i - 1]) / (g[i] - g[i - 1]) : 0;
     return cum[i - 1] + f * (cum[i] - cum[i - 1]);
   };
+  // largest n with C(n) <= v (C is piecewise linear and non-decreasing)
+  auto Cinv = [&](double v) {
+    if (v >= total) return (double) L;
+    const size_t i = std::upper_bound(cum.begin(), cum.end(), v) - cum.begin();   // cum[i - 1] <= v < cum[i]
+    const double d = cum[i] - cum[i - 1];
+    const double f = d > 0 ? (v - cum[i - 1]) / d : 0;
+    return g[i - 1] + f * (g[i] - g[i - 1]);
+  };
   std::vector<int64_t> seg;
   int64_t a = 0;
   seg.push_back(0);
   while (a < L) {
-    double ca = C((double) a);
-    int64_t lo = a + 240, hi = std::min(a + smax, L);
+    const int64_t lo = a + 240, hi = std::min(a + smax, L);
     if (hi <= lo) { a = std::min(a + smax, L); seg.push_back(a); continue; }
-    // largest end with cost <= target (binary search on multiples of 240)
-    int64_t best = lo;
-    if (C((double) hi) - ca <= target) best = hi;
-    else {
-      int64_t l = lo / 240, h = hi / 240;
-      while (l < h) {
-        int64_t m = (l + h + 1) / 2;
-        if (C((double) (m * 240)) - ca <= target) l = m; else h = m - 1;
-      }
-      best = std::max(lo, l * 240);
-    }
+    // the largest end (a multiple of 240, or hi) with cost <= target
+    const double n = Cinv(C((double) a) + target);
+    int64_t best = n >= (double) hi ? hi : (int64_t) (n / 240) * 240;
+    best = std::max(lo, std::min(best, hi));
     a = std::min(best, L);
     seg.push_back(a);
   }
@@ -1757,7 +1769,14 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune_in, cud
   int grid = c.num_sms * ctas;
 
   // segment table: small segments where leaves are dense, full ones elsewhere
-  std::vector<int64_t> seglo = plan_segments(pb, c.tab, L, x_star, pi_sqrt, bglob, (int64_t) words * 240, grid);
+  // the plan depends on the problem and the launch shape only: reused while they repeat
+  const std::vector<int64_t> key = {(int64_t) (uint64_t) x, (int64_t) (uint64_t) (x >> 64), pb.y, pb.z, pb.k,
+                                    (int64_t) pb.gourdon, (int64_t) words, (int64_t) grid};
+  if (c.plan_key != key) {
+    c.plan = plan_segments(pb, c.tab, L, x_star, pi_sqrt, bglob, (int64_t) words * 240, grid);
+    c.plan_key = key;
+  }
+  const std::vector<int64_t>& seglo = c.plan;
   int64_t nseg = (int64_t) seglo.size() - 1;
   DevBuf& segbuf = c.tmp[T_SW_SEG];
   segbuf.alloc(seglo.size() * 8);
