@@ -174,6 +174,7 @@ Ctx::~Ctx()
 {
   for (auto& e : ev) if (e) cudaEventDestroy(e);
   for (auto& e : kev) if (e) cudaEventDestroy(e);
+  if (aux) cudaStreamDestroy(aux);
   if (own_stream && stream) cudaStreamDestroy(stream);
 }
 

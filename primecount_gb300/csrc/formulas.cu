@@ -21,6 +21,10 @@
 #include <algorithm>
 #include <vector>
 
+#include <thread>
+#include <exception>
+#include <mutex>
+#include <cstdlib>
 #include "pcg_internal.hpp"
 #include "dev_common.cuh"
 
@@ -853,6 +857,24 @@ static void ensure_pibig(Ctx& c, int64_t limit, cudaStream_t s)
   c.tab.pibig_limit = limit;
 }
 
+// D runs beside the other terms of pi(x) unless PCG_PI_OVERLAP=0
+static bool pi_overlap()
+{
+  static const bool on = [] {
+    const char* e = getenv("PCG_PI_OVERLAP");
+    return !(e && atoi(e) == 0);
+  }();
+  return on;
+}
+
+// the context's second stream (created on first use)
+static cudaStream_t aux_stream(Ctx& c)
+{
+  std::lock_guard<std::mutex> g(c.aux_mu);
+  if (!c.aux) PCG_CUDA(cudaStreamCreateWithFlags(&c.aux, cudaStreamNonBlocking));
+  return c.aux;
+}
+
 static PiParts pi_gourdon(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s)
 {
   PiParts R;
@@ -869,166 +891,198 @@ static PiParts pi_gourdon(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s)
   R.ms_tables = fnow_ms() - t0;
   const Tables& T = c.tab;
 
-  // ---- D (hard special leaves)
-  {
-    double t1 = fnow_ms();
-    SweepProblem p;
-    p.gourdon = 1;
-    p.x = x;
-    p.y = y;
-    p.z = z;
-    p.k = k;
-    SweepResult r = run_sweep(c, p, tune, s);
-    R.d = r.sum;
-    R.dstats = r.stats;
-    R.launches += r.stats.kernel_launches;
-    R.ms_d = fnow_ms() - t1;
-  }
-
-  // ---- A + C
-  {
-    double t1 = fnow_ms();
-    const u128 xy = x / (u128) y, xz = x / (u128) z;
-    AcParams P;
-    memset(&P, 0, sizeof(P));
-    P.x_lo = (uint64_t) x;
-    P.x_hi = (uint64_t) (x >> 64);
-    P.y = y;
-    P.z = z;
-    P.k = k;
-    P.x_star = x_star;
-    P.x13 = x13;
-    P.sqrtx = sqrtx;
-    P.primes = T.primes.as<uint32_t>();
-    P.pismall = T.pitab.as<uint64_t>();
-    P.pibig = T.pibig.as<uint64_t>();
-    const int64_t pi_sqrtz = host_pi(T, (uint64_t) isqrt((u128) z));
-    P.bA0 = host_pi(T, (uint64_t) x_star);
-    P.bA1 = host_pi(T, (uint64_t) x13);
-    P.bC10 = std::max<int64_t>(k, host_pi(T, (uint64_t) iroot(xz, 3)));
-    P.bC11 = pi_sqrtz;
-    P.bC20 = std::max<int64_t>({k, host_pi(T, (uint64_t) iroot(xy, 3)), pi_sqrtz});
-    P.bC21 = host_pi(T, (uint64_t) x_star);
-    const int64_t nA = std::max<int64_t>(0, P.bA1 - P.bA0);
-    const int64_t nC1 = std::max<int64_t>(0, P.bC11 - P.bC10);
-    const int64_t nC2 = std::max<int64_t>(0, P.bC21 - P.bC20);
-    // C1 products: count q per b, then expand
-    int64_t nQ = 0;
-    DevBuf& qlo = c.tmp[T_AC_QLO];
-    DevBuf& qcnt = c.tmp[T_AC_QCNT];
-    DevBuf& qoff = c.tmp[T_AC_QOFF];
-    std::vector<int64_t> hq;
-    if (nC1 > 0) {
-      qlo.alloc((size_t) nC1 * 8);
-      qcnt.alloc((size_t) nC1 * 8);
-      qoff.alloc((size_t) nC1 * 8);
-      k_c1_qcount<<<(unsigned) ((nC1 + 127) / 128), 128, 0, s>>>(P, qlo.as<int64_t>(), qcnt.as<int64_t>());
-      PCG_CUDA(cudaGetLastError());
-      R.launches++;
-      hq.resize((size_t) nC1);
-      PCG_CUDA(cudaMemcpyAsync(hq.data(), qcnt.p, (size_t) nC1 * 8, cudaMemcpyDeviceToHost, s));
-      PCG_CUDA(cudaStreamSynchronize(s));
-      std::vector<int64_t> off((size_t) nC1);
-      for (int64_t j = 0; j < nC1; j++) { off[(size_t) j] = nQ; nQ += hq[(size_t) j]; }
-      PCG_CUDA(cudaMemcpyAsync(qoff.p, off.data(), (size_t) nC1 * 8, cudaMemcpyHostToDevice, s));
+  // ---- D (hard special leaves) on s and, from a second host thread on the
+  // context's second stream, A + C, B, Phi0 and Sigma: their launches fill
+  // the SMs that the sweep's waves leave idle at their ends
+  auto d_term = [&]() {
+    {
+      double t1 = fnow_ms();
+      SweepProblem p;
+      p.gourdon = 1;
+      p.x = x;
+      p.y = y;
+      p.z = z;
+      p.k = k;
+      SweepResult r = run_sweep(c, p, tune, s);
+      R.d = r.sum;
+      R.dstats = r.stats;
+      R.launches += r.stats.kernel_launches;
+      R.ms_d = fnow_ms() - t1;
     }
-    const int64_t nout = nA + nC1 + nQ + nC2;
-    i128 sum = 0;
-    if (nout > 0) {
-      DevBuf& outs = c.tmp[T_AC_OUTS];
-      outs.alloc((size_t) nout * sizeof(PairOuter));
-      PairOuter* o = outs.as<PairOuter>();
-      if (nA) k_outer_A<<<(unsigned) ((nA + 127) / 128), 128, 0, s>>>(P, o);
-      if (nC1) k_outer_C1<<<(unsigned) ((nC1 + 127) / 128), 128, 0, s>>>(P, o + nA);
-      if (nQ) k_c1_expand<<<(unsigned) ((nC1 + 127) / 128), 128, 0, s>>>(P, qlo.as<int64_t>(), qcnt.as<int64_t>(),
-                                                                          qoff.as<int64_t>(), o + nA + nC1);
-      if (nC2) k_outer_C2<<<(unsigned) ((nC2 + 127) / 128), 128, 0, s>>>(P, o + nA + nC1 + nQ);
-      PCG_CUDA(cudaGetLastError());
-      R.launches += 4;
-      sum = run_pairs(c, o, nout, s, &R.launches);
-    }
-    R.ac = sum;
-    R.ms_ac = fnow_ms() - t1;
-  }
-
-  // ---- B = sum over primes y < p <= sqrt(x) of pi(x / p)
-  {
-    double t1 = fnow_ms();
-    const int64_t n0 = (int64_t) (x / (u128) sqrtx);   // smallest x / p
-    const int64_t n1 = (int64_t) (x / (u128) (y + 1)) + 1;  // x / p < n1 for p > y
-    i128 B = 0;
-    if (sqrtx > y && n1 > n0) {
-      PsOut o = run_psieve(c, x, n0, n1, true, y, sqrtx, s, &R.launches);
-      // pi(lo0 - 1) from the PiTable up to sqrt(x) (lo0 >= sqrt(x) > 1e5 here)
-      i128 run = 0;
-      if (o.lo0 >= 7) run = pi_lookup(c, std::vector<uint64_t>{(uint64_t) (o.lo0 - 1)}, s)[0];
-      for (int64_t i = 0; i < o.nseg; i++) {
-        B += (i128) o.l[(size_t) i] + (i128) o.m[(size_t) i] * run;
-        run += o.c[(size_t) i];
+  };
+  auto other_terms = [&](cudaStream_t s, uint64_t* nl) {
+    // ---- A + C
+    {
+      double t1 = fnow_ms();
+      const u128 xy = x / (u128) y, xz = x / (u128) z;
+      AcParams P;
+      memset(&P, 0, sizeof(P));
+      P.x_lo = (uint64_t) x;
+      P.x_hi = (uint64_t) (x >> 64);
+      P.y = y;
+      P.z = z;
+      P.k = k;
+      P.x_star = x_star;
+      P.x13 = x13;
+      P.sqrtx = sqrtx;
+      P.primes = T.primes.as<uint32_t>();
+      P.pismall = T.pitab.as<uint64_t>();
+      P.pibig = T.pibig.as<uint64_t>();
+      const int64_t pi_sqrtz = host_pi(T, (uint64_t) isqrt((u128) z));
+      P.bA0 = host_pi(T, (uint64_t) x_star);
+      P.bA1 = host_pi(T, (uint64_t) x13);
+      P.bC10 = std::max<int64_t>(k, host_pi(T, (uint64_t) iroot(xz, 3)));
+      P.bC11 = pi_sqrtz;
+      P.bC20 = std::max<int64_t>({k, host_pi(T, (uint64_t) iroot(xy, 3)), pi_sqrtz});
+      P.bC21 = host_pi(T, (uint64_t) x_star);
+      const int64_t nA = std::max<int64_t>(0, P.bA1 - P.bA0);
+      const int64_t nC1 = std::max<int64_t>(0, P.bC11 - P.bC10);
+      const int64_t nC2 = std::max<int64_t>(0, P.bC21 - P.bC20);
+      // C1 products: count q per b, then expand
+      int64_t nQ = 0;
+      DevBuf& qlo = c.tmp[T_AC_QLO];
+      DevBuf& qcnt = c.tmp[T_AC_QCNT];
+      DevBuf& qoff = c.tmp[T_AC_QOFF];
+      std::vector<int64_t> hq;
+      if (nC1 > 0) {
+        qlo.alloc((size_t) nC1 * 8);
+        qcnt.alloc((size_t) nC1 * 8);
+        qoff.alloc((size_t) nC1 * 8);
+        k_c1_qcount<<<(unsigned) ((nC1 + 127) / 128), 128, 0, s>>>(P, qlo.as<int64_t>(), qcnt.as<int64_t>());
+        PCG_CUDA(cudaGetLastError());
+        (*nl)++;
+        hq.resize((size_t) nC1);
+        PCG_CUDA(cudaMemcpyAsync(hq.data(), qcnt.p, (size_t) nC1 * 8, cudaMemcpyDeviceToHost, s));
+        PCG_CUDA(cudaStreamSynchronize(s));
+        std::vector<int64_t> off((size_t) nC1);
+        for (int64_t j = 0; j < nC1; j++) { off[(size_t) j] = nQ; nQ += hq[(size_t) j]; }
+        PCG_CUDA(cudaMemcpyAsync(qoff.p, off.data(), (size_t) nC1 * 8, cudaMemcpyHostToDevice, s));
       }
+      const int64_t nout = nA + nC1 + nQ + nC2;
+      i128 sum = 0;
+      if (nout > 0) {
+        DevBuf& outs = c.tmp[T_AC_OUTS];
+        outs.alloc((size_t) nout * sizeof(PairOuter));
+        PairOuter* o = outs.as<PairOuter>();
+        if (nA) k_outer_A<<<(unsigned) ((nA + 127) / 128), 128, 0, s>>>(P, o);
+        if (nC1) k_outer_C1<<<(unsigned) ((nC1 + 127) / 128), 128, 0, s>>>(P, o + nA);
+        if (nQ) k_c1_expand<<<(unsigned) ((nC1 + 127) / 128), 128, 0, s>>>(P, qlo.as<int64_t>(), qcnt.as<int64_t>(),
+                                                                            qoff.as<int64_t>(), o + nA + nC1);
+        if (nC2) k_outer_C2<<<(unsigned) ((nC2 + 127) / 128), 128, 0, s>>>(P, o + nA + nC1 + nQ);
+        PCG_CUDA(cudaGetLastError());
+        *nl += 4;
+        sum = run_pairs(c, o, nout, s, nl);
+      }
+      R.ac = sum;
+      R.ms_ac = fnow_ms() - t1;
     }
-    R.b = B;
-    R.ms_b = fnow_ms() - t1;
-  }
 
-  // ---- Phi0
-  {
-    double t1 = fnow_ms();
-    const int64_t size = wheel2310().to_index((uint64_t) z) + 1;
-    const int grid = c.num_sms * 8;
-    DevBuf& part = c.tmp[T_PHI0_PART];
-    part.alloc((size_t) grid * 16);
-    PCG_CUDA(cudaMemsetAsync(part.p, 0, (size_t) grid * 16, s));
-    PhiTab PT = phi_tab(c);
-    if (T.fd_bytes == 2)
-      k_phi0<uint16_t><<<grid, 256, 0, s>>>((uint64_t) x, (uint64_t) (x >> 64), T.factor_d.as<uint16_t>(), size,
-                                            (uint32_t) (2 * k + 1), (uint64_t) T.h_primes[(size_t) k], PT, T.coprime.as<uint16_t>(), part.as<i128>());
-    else
-      k_phi0<uint32_t><<<grid, 256, 0, s>>>((uint64_t) x, (uint64_t) (x >> 64), T.factor_d.as<uint32_t>(), size,
-                                            (uint32_t) (2 * k + 1), (uint64_t) T.h_primes[(size_t) k], PT, T.coprime.as<uint16_t>(), part.as<i128>());
-    PCG_CUDA(cudaGetLastError());
-    R.launches++;
-    R.phi0 = sum_partials(part, grid, s);
-    R.ms_phi0 = fnow_ms() - t1;
-  }
+    // ---- B = sum over primes y < p <= sqrt(x) of pi(x / p)
+    {
+      double t1 = fnow_ms();
+      const int64_t n0 = (int64_t) (x / (u128) sqrtx);   // smallest x / p
+      const int64_t n1 = (int64_t) (x / (u128) (y + 1)) + 1;  // x / p < n1 for p > y
+      i128 B = 0;
+      if (sqrtx > y && n1 > n0) {
+        PsOut o = run_psieve(c, x, n0, n1, true, y, sqrtx, s, nl);
+        // pi(lo0 - 1) from the PiTable up to sqrt(x) (lo0 >= sqrt(x) > 1e5 here)
+        i128 run = 0;
+        if (o.lo0 >= 7) run = pi_lookup(c, std::vector<uint64_t>{(uint64_t) (o.lo0 - 1)}, s)[0];
+        for (int64_t i = 0; i < o.nseg; i++) {
+          B += (i128) o.l[(size_t) i] + (i128) o.m[(size_t) i] * run;
+          run += o.c[(size_t) i];
+        }
+      }
+      R.b = B;
+      R.ms_b = fnow_ms() - t1;
+    }
 
-  // ---- Sigma (Sigma.cpp:25-140)
-  {
-    double t1 = fnow_ms();
-    const i128 a = host_pi(T, (uint64_t) y);
-    const i128 b = host_pi(T, (uint64_t) x13);
-    const int64_t sqrt_xy = isqrt(x / (u128) y);
-    std::vector<uint64_t> q;
-    q.push_back((uint64_t) sqrtx);
-    q.push_back((uint64_t) sqrt_xy);
-    // primes in (x_star, x^(1/3)]: arguments of Sigma4..6
-    const int64_t i0 = host_pi(T, (uint64_t) x_star) + 1, i1 = host_pi(T, (uint64_t) x13);
-    for (int64_t i = i0; i <= i1; i++) {
-      const u128 p = T.h_primes[(size_t) i];
-      if ((int64_t) p <= sqrt_xy) q.push_back((uint64_t) (x / (p * (u128) y)));
-      else q.push_back((uint64_t) (x / (p * p)));
-      q.push_back((uint64_t) isqrt(x / p));
+    // ---- Phi0
+    {
+      double t1 = fnow_ms();
+      const int64_t size = wheel2310().to_index((uint64_t) z) + 1;
+      const int grid = c.num_sms * 8;
+      DevBuf& part = c.tmp[T_PHI0_PART];
+      part.alloc((size_t) grid * 16);
+      PCG_CUDA(cudaMemsetAsync(part.p, 0, (size_t) grid * 16, s));
+      PhiTab PT = phi_tab(c);
+      if (T.fd_bytes == 2)
+        k_phi0<uint16_t><<<grid, 256, 0, s>>>((uint64_t) x, (uint64_t) (x >> 64), T.factor_d.as<uint16_t>(), size,
+                                              (uint32_t) (2 * k + 1), (uint64_t) T.h_primes[(size_t) k], PT, T.coprime.as<uint16_t>(), part.as<i128>());
+      else
+        k_phi0<uint32_t><<<grid, 256, 0, s>>>((uint64_t) x, (uint64_t) (x >> 64), T.factor_d.as<uint32_t>(), size,
+                                              (uint32_t) (2 * k + 1), (uint64_t) T.h_primes[(size_t) k], PT, T.coprime.as<uint16_t>(), part.as<i128>());
+      PCG_CUDA(cudaGetLastError());
+      (*nl)++;
+      R.phi0 = sum_partials(part, grid, s);
+      R.ms_phi0 = fnow_ms() - t1;
     }
-    std::vector<int64_t> r = pi_lookup(c, q, s);
-    const i128 pi_sqrtx = r[0];
-    const i128 cc = r[1];
-    const i128 d = host_pi(T, (uint64_t) x_star);
-    i128 s0 = a - 1 + (pi_sqrtx * (pi_sqrtx - 1)) / 2 - (a * (a - 1)) / 2;
-    i128 s1 = (a - b) * (a - b - 1) / 2;
-    i128 s2 = a * (b - cc - (cc * (cc - 3)) / 2 + (d * (d - 3)) / 2);
-    i128 s3 = (b * (b - 1) * (2 * b - 1)) / 6 - b - (d * (d - 1) * (2 * d - 1)) / 6 + d;
-    i128 s4 = 0, s5 = 0, s6 = 0;
-    size_t j = 2;
-    for (int64_t i = i0; i <= i1; i++) {
-      const int64_t p = T.h_primes[(size_t) i];
-      if (p <= sqrt_xy) s4 += r[j]; else s5 += r[j];
-      j++;
-      s6 += (i128) r[j] * r[j];
-      j++;
+
+    // ---- Sigma (Sigma.cpp:25-140)
+    {
+      double t1 = fnow_ms();
+      const i128 a = host_pi(T, (uint64_t) y);
+      const i128 b = host_pi(T, (uint64_t) x13);
+      const int64_t sqrt_xy = isqrt(x / (u128) y);
+      std::vector<uint64_t> q;
+      q.push_back((uint64_t) sqrtx);
+      q.push_back((uint64_t) sqrt_xy);
+      // primes in (x_star, x^(1/3)]: arguments of Sigma4..6
+      const int64_t i0 = host_pi(T, (uint64_t) x_star) + 1, i1 = host_pi(T, (uint64_t) x13);
+      for (int64_t i = i0; i <= i1; i++) {
+        const u128 p = T.h_primes[(size_t) i];
+        if ((int64_t) p <= sqrt_xy) q.push_back((uint64_t) (x / (p * (u128) y)));
+        else q.push_back((uint64_t) (x / (p * p)));
+        q.push_back((uint64_t) isqrt(x / p));
+      }
+      std::vector<int64_t> r = pi_lookup(c, q, s);
+      const i128 pi_sqrtx = r[0];
+      const i128 cc = r[1];
+      const i128 d = host_pi(T, (uint64_t) x_star);
+      i128 s0 = a - 1 + (pi_sqrtx * (pi_sqrtx - 1)) / 2 - (a * (a - 1)) / 2;
+      i128 s1 = (a - b) * (a - b - 1) / 2;
+      i128 s2 = a * (b - cc - (cc * (cc - 3)) / 2 + (d * (d - 3)) / 2);
+      i128 s3 = (b * (b - 1) * (2 * b - 1)) / 6 - b - (d * (d - 1) * (2 * d - 1)) / 6 + d;
+      i128 s4 = 0, s5 = 0, s6 = 0;
+      size_t j = 2;
+      for (int64_t i = i0; i <= i1; i++) {
+        const int64_t p = T.h_primes[(size_t) i];
+        if (p <= sqrt_xy) s4 += r[j]; else s5 += r[j];
+        j++;
+        s6 += (i128) r[j] * r[j];
+        j++;
+      }
+      R.sigma = s0 + s1 + s2 + s3 + s4 * a + s5 - s6;
+      R.ms_sigma = fnow_ms() - t1;
     }
-    R.sigma = s0 + s1 + s2 + s3 + s4 * a + s5 - s6;
-    R.ms_sigma = fnow_ms() - t1;
+  };
+  uint64_t launches2 = 0;
+  if (pi_overlap()) {
+    cudaStream_t s2 = aux_stream(c);
+    PCG_CUDA(cudaEventRecord(c.ev[2], s));          // the tables are built on s
+    PCG_CUDA(cudaStreamWaitEvent(s2, c.ev[2], 0));
+    std::exception_ptr err;
+    std::thread th([&] {
+      try {
+        PCG_CUDA(cudaSetDevice(c.device));
+        other_terms(s2, &launches2);
+      } catch (...) {
+        err = std::current_exception();
+      }
+    });
+    try {
+      d_term();
+    } catch (...) {
+      th.join();
+      throw;
+    }
+    th.join();
+    if (err) std::rethrow_exception(err);
+  } else {
+    d_term();
+    other_terms(s, &launches2);
   }
+  R.launches += launches2;
   R.pi = R.ac - R.b + R.d + R.phi0 + R.sigma;
   return R;
 }

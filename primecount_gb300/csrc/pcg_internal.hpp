@@ -9,6 +9,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <string>
+#include <mutex>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -194,6 +195,9 @@ struct Ctx {
   std::vector<cudaEvent_t> kev;   // per-launch timing events of the sweep
   // the last segment plan of the sweep and the problem and launch shape it was made for
   std::vector<int64_t> plan, plan_key;
+  // second stream for work that runs beside the sweep (pi(x)'s other terms)
+  cudaStream_t aux = nullptr;
+  std::mutex aux_mu;
   ~Ctx();
 };
 

@@ -37,10 +37,10 @@ PCG_EAGAIN = 9   # refused: the admitted backlog would exceed the latency budget
 
 def est_seconds(kind, x, a=None):
     """GPU-seconds of one query on one GB300 with resident tables (measured:
-    pi(1e16) 0.03 s, pi(1e18) 0.24 s, pi(1e20) 4.2 s; phi(x <= 1e16, a) a few ms)."""
+    pi(1e16) 0.02 s, pi(1e18) 0.17 s, pi(1e20) 3.0 s; phi(x <= 1e16, a) a few ms)."""
     x = max(int(x), 2)
     if kind == "pi":
-        return 0.004 + 4.2 * (x / 1e20) ** 0.6
+        return 0.004 + 3.0 * (x / 1e20) ** 0.6
     return 0.002 + 0.05 * (x / 1e16) ** 0.5
 
 
