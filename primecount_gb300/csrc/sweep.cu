@@ -433,6 +433,11 @@ __device__ __forceinline__ bool cross_off(uint64_t* bits, uint32_t w, uint32_t r
 #define REC_NONE 0xFFFFFFFFu
 // table entries per thread and round of the record phase
 #define PA_UNROLL 8
+// levels with at most this many record slots in a window are answered
+// without a chunk prefix scan
+#ifndef SMALL_QUERIES
+#define SMALL_QUERIES 16
+#endif
 // consecutive levels with p^3 >= high answered together (see k_sweep)
 #define GROUP_MAX 64
 
@@ -1037,19 +1042,46 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
           const int rz = (int) (dmin(lz, wend) - w0);           // end of the level's window records
           const int rb = li == clev ? s_ncomp[win & 1] : rz;   // end of those still to answer
           if (rb > ra) {
-            if (dirty) { scan_chunks(ccount, pref, nch, wtmp); dirty = false; }
-            if (ra + 32 * warp < rb) {
-              int smu_t = 0;
-              for (int k2 = ra + tid; k2 < rb; k2 += NT) {
+            if (dirty && rb - ra <= SMALL_QUERIES) {
+              // a few records: a warp per record sums the chunk counts below
+              // the record's chunk itself, instead of a block-wide prefix
+              // scan (the prefix array stays out of date)
+              int smu_w = 0;
+              for (int k2 = ra + warp; k2 < rb; k2 += NT / 32) {
                 const uint32_t r = rec[k2];
-                if (r != REC_NONE) {
-                  const uint32_t c = query(bits, pref, r & 0x3FFFFFFFu);
-                  if (r & (1u << 30)) { lsum -= c; smu_t--; }
-                  else { lsum += c; smu_t++; }
+                if (r == REC_NONE) continue;
+                const uint32_t off = r & 0x3FFFFFFFu;
+                const uint32_t wd = off / 240, ch = wd >> 3, kw = wd & 7;
+                uint32_t part = 0;
+                for (uint32_t i = 4 * lane; i < ch; i += 128) {
+                  const uint4 v = *(const uint4*) (ccount + i);
+                  part += v.x + (i + 1 < ch ? v.y : 0u) + (i + 2 < ch ? v.z : 0u) + (i + 3 < ch ? v.w : 0u);
                 }
+                if (lane < 8) {
+                  const uint64_t v = bits[8 * ch + lane];
+                  const uint32_t j = (uint32_t) lane;
+                  part += (uint32_t) __popcll(j < kw ? v : (j == kw ? (v & mask_le(off - wd * 240)) : 0ull));
+                }
+                const uint32_t c = __reduce_add_sync(0xffffffffu, part);
+                if (r & (1u << 30)) { if (lane == 0) lsum -= c; smu_w--; }
+                else { if (lane == 0) lsum += c; smu_w++; }
               }
-              smu_t = __reduce_add_sync(0xffffffffu, smu_t);
-              if (lane == 0 && smu_t) atomicAdd(&s_smu, smu_t);
+              if (lane == 0 && smu_w) atomicAdd(&s_smu, smu_w);
+            } else {
+              if (dirty) { scan_chunks(ccount, pref, nch, wtmp); dirty = false; }
+              if (ra + 32 * warp < rb) {
+                int smu_t = 0;
+                for (int k2 = ra + tid; k2 < rb; k2 += NT) {
+                  const uint32_t r = rec[k2];
+                  if (r != REC_NONE) {
+                    const uint32_t c = query(bits, pref, r & 0x3FFFFFFFu);
+                    if (r & (1u << 30)) { lsum -= c; smu_t--; }
+                    else { lsum += c; smu_t++; }
+                  }
+                }
+                smu_t = __reduce_add_sync(0xffffffffu, smu_t);
+                if (lane == 0 && smu_t) atomicAdd(&s_smu, smu_t);
+              }
             }
             __syncthreads();
           }
