@@ -954,9 +954,46 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                 s_gsmu[tid] = 0;
                 s_gmag[tid] = A.pmagic[b0 + li + tid];
               }
-              if (rb > ra && dirty) { scan_chunks(ccount, pref, nch, wtmp); dirty = false; }
+              // a few records: a warp per record, its lanes summing the chunk
+              // counts below the record's chunk and the removals of one group
+              // level each (no prefix scan)
+              const bool few = dirty && rb > ra && rb - ra <= SMALL_QUERIES;
+              if (rb > ra && dirty && !few) { scan_chunks(ccount, pref, nch, wtmp); dirty = false; }
               else __syncthreads();
-              if (rb > ra) {
+              if (few) {
+                for (int k2 = ra + warp; k2 < rb; k2 += NT / 32) {
+                  const uint32_t r = rec[k2];
+                  if (r == REC_NONE) continue;
+                  int lv = li;
+                  while (loff[lv + 1] <= w0 + k2) lv++;
+                  const uint32_t off = r & 0x3FFFFFFFu;
+                  const uint64_t n = (uint64_t) low + off;
+                  const uint32_t wd = off / 240, ch = wd >> 3, kw = wd & 7;
+                  uint32_t part = 0;
+                  for (uint32_t i = 4 * lane; i < ch; i += 128) {
+                    const uint4 v = *(const uint4*) (ccount + i);
+                    part += v.x + (i + 1 < ch ? v.y : 0u) + (i + 2 < ch ? v.z : 0u) + (i + 3 < ch ? v.w : 0u);
+                  }
+                  if (lane < 8) {
+                    const uint64_t v = bits[8 * ch + lane];
+                    const uint32_t j = (uint32_t) lane;
+                    part += (uint32_t) __popcll(j < kw ? v : (j == kw ? (v & mask_le(off - wd * 240)) : 0ull));
+                  }
+                  // the numbers <= n removed by the levels li .. lv-1, one per lane
+                  for (int b = li + lane; b < lv; b += 32) {
+                    const uint64_t pb = lp[b].prime;
+                    if (pb <= n && pb >= (uint64_t) low) part--;
+                    const int64_t d = dpi(A.pitab, div_magic(n, pb, s_gmag[b - li])) - (int64_t) s_pc[b];
+                    if (d > 0) part -= (uint32_t) d;
+                  }
+                  // the count is below 2^32: the sum modulo 2^32 is exact
+                  const uint32_t c = __reduce_add_sync(0xffffffffu, part);
+                  if (lane == 0) {
+                    if (r & (1u << 30)) { lsum -= c; atomicAdd(&s_gsmu[lv - li], -1); }
+                    else { lsum += c; atomicAdd(&s_gsmu[lv - li], 1); }
+                  }
+                }
+              } else if (rb > ra) {
                 int lv = li;
                 for (int k2 = ra + tid; k2 < rb; k2 += NT) {
                   const int64_t pos = w0 + k2;
