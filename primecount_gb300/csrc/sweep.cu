@@ -433,10 +433,10 @@ __device__ __forceinline__ bool cross_off(uint64_t* bits, uint32_t w, uint32_t r
 #define REC_NONE 0xFFFFFFFFu
 // table entries per thread and round of the record phase
 #define PA_UNROLL 8
-// levels with at most this many record slots in a window are answered
-// without a chunk prefix scan
+// levels (and groups of levels) with at most this many record slots in a
+// window are answered without a chunk prefix scan
 #ifndef SMALL_QUERIES
-#define SMALL_QUERIES 16
+#define SMALL_QUERIES 32
 #endif
 // consecutive levels with p^3 >= high answered together (see k_sweep)
 #define GROUP_MAX 64
