@@ -347,7 +347,9 @@ def main():
             c3.close()
         pi_line = {"x": args.x, "pi": str(pv), "seconds": min(ts), "seconds_all": ts,
                    "terms_ms": {"D": s3["d_ms"], "AC": s3["ac_ms"], "B": s3["b_ms"], "Phi0": s3["phi0_ms"],
-                                "Sigma": s3["sigma_ms"], "tables": s3["table_ms"]}}
+                                "Sigma": s3["sigma_ms"], "tables": s3["table_ms"]},
+                   "terms_note": "a new context per call (tables built inside it); D runs beside A+C, B, Phi0 "
+                                 "and Sigma, so the term times are wall times of the two host threads"}
 
     batch = run_batch(args, pcg) if args.batch > 0 and rank == 0 else None
     serve = None
