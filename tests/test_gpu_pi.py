@@ -90,3 +90,20 @@ def test_pi_1e20_and_1e21(pcg, golden):
     for n in (20, 21):
         x = 10 ** n
         assert pcg.pi(x) == golden["pi_pow10"][str(x)], n
+
+
+def test_pi_terms_in_sequence(pcg, golden):
+    # PCG_PI_OVERLAP=0 runs D and the other terms one after the other instead of
+    # side by side on two streams: same values (read once per process, hence a child)
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    xs = [10 ** 15, 10 ** 17, 123456789012345678]
+    code = ("import sys; sys.path.insert(0, %r); import primecount_gb300 as p; "
+            "print(' '.join(str(p.pi(x)) for x in %r))" % (root, xs))
+    env = dict(os.environ, PCG_PI_OVERLAP="0")
+    out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.split() == [str(pcg.pi(x)) for x in xs]
+    assert int(out.stdout.split()[0]) == golden["pi_pow10"][str(10 ** 15)]
