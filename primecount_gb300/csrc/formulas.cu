@@ -895,20 +895,18 @@ static PiParts pi_gourdon(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s)
   // context's second stream, A + C, B, Phi0 and Sigma: their launches fill
   // the SMs that the sweep's waves leave idle at their ends
   auto d_term = [&]() {
-    {
-      double t1 = fnow_ms();
-      SweepProblem p;
-      p.gourdon = 1;
-      p.x = x;
-      p.y = y;
-      p.z = z;
-      p.k = k;
-      SweepResult r = run_sweep(c, p, tune, s);
-      R.d = r.sum;
-      R.dstats = r.stats;
-      R.launches += r.stats.kernel_launches;
-      R.ms_d = fnow_ms() - t1;
-    }
+    double t1 = fnow_ms();
+    SweepProblem p;
+    p.gourdon = 1;
+    p.x = x;
+    p.y = y;
+    p.z = z;
+    p.k = k;
+    SweepResult r = run_sweep(c, p, tune, s);
+    R.d = r.sum;
+    R.dstats = r.stats;
+    R.launches += r.stats.kernel_launches;
+    R.ms_d = fnow_ms() - t1;
   };
   auto other_terms = [&](cudaStream_t s, uint64_t* nl) {
     // ---- A + C

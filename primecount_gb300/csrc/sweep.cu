@@ -1211,7 +1211,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
 }
 
 // ---- phi offsets: acc[b] += sum_s M(s, b) * sum_{s'<s} C(s', b), in segment order.
-// A block takes 32 levels; its CW warps take consecutive runs of the wave's
+// A block takes 32 levels; its COMBINE_WARPS warps take consecutive runs of the wave's
 // segments and sum them from a local count of 0, then the runs are chained:
 // a run k whose segments see the count R_k + r (r its local prefix) adds
 // a_k + ms_k R_k, with a_k = sum M r and ms_k = sum M over the run.
