@@ -61,7 +61,8 @@ typedef struct pcg_ctx pcg_ctx;
 
 /* Options of one call.  A NULL pcg_opts* means all defaults. */
 typedef struct {
-  pcg_ctx* ctx;          /* NULL: the library's default context of the current device */
+  pcg_ctx* ctx;          /* NULL: the library's default context of the current device;
+                            calls on one context run one at a time                    */
   void* stream;          /* cudaStream_t to launch on; NULL: the context's stream      */
   int threads;           /* batches: worker contexts on the GPU (0 = 8); else unused   */
   int print;             /* reference is_print: print variables and timings            */

@@ -251,6 +251,7 @@ pcg_status guarded_call(const pcg_opts* opts, void (*fn)(Ctx&, cudaStream_t, voi
   Ctx* cp = nullptr;
   return guard(nullptr, [&] {
     cp = ctx_from(opts);
+    std::lock_guard<std::recursive_mutex> lk(cp->call_mu);
     cp->last_error.clear();
     try {
       fn(*cp, stream_from(*cp, opts), arg);
@@ -390,6 +391,7 @@ static pcg_status hard_leaves(bool gourdon, pcg_i128 xi, int64_t y, int64_t z, i
   Ctx* cp = nullptr;
   return guard(nullptr, [&] {
     cp = ctx_from(opts);
+    std::lock_guard<std::recursive_mutex> lk(cp->call_mu);
     Ctx& c = *cp;
     c.last_error.clear();
     if (xi.hi < 0) fail(PCG_EINVAL, "x must be >= 0");
@@ -432,6 +434,7 @@ static pcg_status hard_leaves_shard(bool gourdon, pcg_i128 xi, int64_t y, int64_
   Ctx* cp = nullptr;
   return guard(nullptr, [&] {
     cp = ctx_from(opts);
+    std::lock_guard<std::recursive_mutex> lk(cp->call_mu);
     Ctx& c = *cp;
     c.last_error.clear();
     if (xi.hi < 0) fail(PCG_EINVAL, "x must be >= 0");
@@ -483,6 +486,7 @@ pcg_status pcg_autotune(pcg_i128 xi, const pcg_opts* opts, pcg_tuning* best)
   Ctx* cp = nullptr;
   return guard(nullptr, [&] {
     cp = ctx_from(opts);
+    std::lock_guard<std::recursive_mutex> lk(cp->call_mu);
     Ctx& c = *cp;
     c.last_error.clear();
     if (xi.hi < 0) fail(PCG_EINVAL, "x must be >= 0");
@@ -562,6 +566,7 @@ pcg_status pcg_D_noalloc(pcg_ctx* ctx, pcg_i128 xi, int64_t y, int64_t z, int64_
   if (!out) return PCG_EINVAL;
   return guard(ctx, [&] {
     if (!ctx) fail(PCG_EINVAL, "pcg_D_noalloc needs a context created with pcg_ctx_create");
+    std::lock_guard<std::recursive_mutex> lk(ctx->call_mu);
     Ctx& c = *ctx;
     c.last_error.clear();
     if (xi.hi < 0) fail(PCG_EINVAL, "x must be >= 0");

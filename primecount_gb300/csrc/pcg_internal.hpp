@@ -198,6 +198,9 @@ struct Ctx {
   // second stream for work that runs beside the sweep (pi(x)'s other terms)
   cudaStream_t aux = nullptr;
   std::mutex aux_mu;
+  // calls on one context run one at a time (threads wanting concurrency use
+  // one context each, as the batch and serving forms do)
+  std::recursive_mutex call_mu;
   ~Ctx();
 };
 

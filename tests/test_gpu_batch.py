@@ -58,3 +58,29 @@ def test_server_refuses_above_max_and_cancels(pcg):
                 assert q.future.exception().status == 7
     finally:
         srv.close()
+
+
+def test_threads_sharing_the_default_context(pcg, golden):
+    # calls on one context run one at a time: threads calling through the
+    # default context concurrently get the values of calls made alone
+    import threading
+    pows = {int(k): v for k, v in golden["pi_pow10"].items() if 10 ** 11 <= int(k) <= 10 ** 15}
+    xs = sorted(pows) * 3
+    got = {}
+    errs = []
+
+    def work(i, x):
+        try:
+            got[i] = pcg.pi(x) if i % 2 == 0 else pcg.D_default(x)
+        except Exception as e:  # reported below
+            errs.append(e)
+
+    th = [threading.Thread(target=work, args=(i, x)) for i, x in enumerate(xs)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not errs, errs
+    for i, x in enumerate(xs):
+        want = pows[x] if i % 2 == 0 else pcg.D_default(x)
+        assert got[i] == want, (i, x)
