@@ -289,7 +289,6 @@ static void check_hard_args(u128 x, int64_t y, int64_t z, int64_t k, bool gourdo
 {
   if (y < 1 || z < 1 || k < 0) fail(PCG_EINVAL, "y, z must be >= 1 and k >= 0");
   if (x > ((u128) y << 62)) fail(PCG_ERANGE, gourdon ? "D(x): x is too large" : "S2_hard(x): x is too large");
-  if (gourdon && z > 386083ll * 386083 - 1 && false) fail(PCG_ERANGE, "z must be <= FactorTableD::max()");
 }
 
 extern "C" {
