@@ -21,9 +21,11 @@
 //    adds sum_b sum_s M(s, b) * sum_{s'<s} C(s', b).  This replaces the
 //    reference's per-chunk phi_vector (src/phi_vector.cpp:302-336) and makes
 //    every segment independent: no second sieve pass is needed.
-//  * Leaf queries are random-order popcount prefix queries against a
-//    per-64-word chunk prefix array rebuilt (block scan) only when the
-//    bitmap changed since the last leaf level.
+//  * Leaf queries are random-order popcount prefix queries.  The counts of
+//    the 8-word chunks are kept current by the cross-off; a level's queries
+//    read their exclusive prefix, rebuilt by a block scan when the bitmap
+//    changed since the last scan, or, for a level with few records, a warp
+//    per record sums the chunk counts below it.
 //  * Segments are handed out by an atomic counter (device work queue, the
 //    role of LoadBalancerS2, src/LoadBalancerS2.cpp:139-193) in waves whose
 //    C/M matrices fit a fixed HBM budget.
