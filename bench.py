@@ -104,6 +104,22 @@ def profile_traffic():
     return None
 
 
+def profile_issue():
+    """Issue-slot use of k_sweep (ncu smsp__issue_active, % of peak) in a sparse
+    and a dense wave of D(1e19), from the committed capture summary: the
+    kernel is bound by the per-level chain and integer issue, not by HBM."""
+    p = os.path.join(ROOT, "profiles", "k_sweep_D1e19.md")
+    try:
+        for line in open(p):
+            if "smsp__issue_active" in line:
+                cells = [c.strip() for c in line.strip().strip("|").split("|")]
+                return {"sparse_wave_pct": float(cells[1].split()[0]), "dense_wave_pct": float(cells[2].split()[0]),
+                        "source": "profiles/k_sweep_D1e19.md"}
+    except (OSError, ValueError, IndexError):
+        return None
+    return None
+
+
 def cpu_baseline(p, threads, target_s=12.0):
     """Oracle restatement of the reference's chunk loop, timed on a sample of
     D(1e20): nchunks sub-intervals starting at c / nchunks of [0, x/z), all
@@ -380,7 +396,8 @@ def main():
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
             "kernel": "k_sweep", "alg_bytes_per_launch": alg_bytes / launches_call,
-            "launch_ms": k_ms_call / launches_call, "launches_per_step": launches_call}
+            "launch_ms": k_ms_call / launches_call, "launches_per_step": launches_call,
+            "issue_active": profile_issue()}
     cpu = None
     if not args.no_cpu and X == 10 ** 20:
         cpu = cpu_baseline(p, os.cpu_count() or 1)
