@@ -11,16 +11,27 @@ value        device-timed (CUDA events on the launching stream), tables
 e2e          the C-ABI call pcg_D on a fresh context: table construction,
              host->device parameter copies, the sweep and the device->host
              result copy, host wall clock.
-roofline     the sieve/leaf kernel (k_sweep): algorithmic table bytes
-             (2 B per FactorTable entry read, 4 B per two-prime leaf,
-             8 B per leaf for the divisor's reciprocal, 16 B per
-             (segment, b) PiTable/level step) over its launch time; traffic
-             = DRAM bytes per launch from the committed ncu capture.
-cpu_baseline the oracle's restatement of the reference's chunk loop on this
-             host's cores, timed on an evenly spread sample of the same
-             interval and scaled to the whole interval.
+roofline     the sieve/leaf kernel (k_sweep) against the measured HBM copy
+             peak, with the algorithmic bytes of the hot-path table: 2 B per
+             FactorTable entry read, 4 B per two-prime leaf (its prime),
+             16 B per (segment, b) step (PiTable word of the level bounds),
+             over its CUDA-event launch time; the 8 B reciprocal per leaf is
+             implementation traffic, reported apart.  traffic = DRAM bytes
+             per launch, scaled from the committed ncu capture of a smaller
+             D by the algorithmic bytes.  int_ops: algorithmic integer and
+             shared-memory operations (per leaf one division and one prefix
+             query of a counter load and up to 8 popcounts; per cross-off
+             one shared-memory read-modify-write) against the SMs' lane
+             issue rate.
+cpu_baseline the reference's own D() (its CLI --D, OpenMP on all host
+             threads, built from its sources by oracle/ref.mk with its
+             run-time SIMD dispatch) timed once on the whole workload; the
+             oracle's restatement on a sample when the reference build is
+             missing (kind "port").
 
---impl reference: the CPU reference arm (the oracle port, all host threads).
+--impl reference: the reference's own D(1e20) on all host threads, one
+             whole evaluation per timed step (the warm-up steps run D at
+             x / 1000); this arm imports nothing of primecount_gb300.
 --gpus N > 1 (torchrun, NCCL): one D(1e20) over N GPUs -- rank r sweeps
              shard r of the segment plan (pcg_D_shard), then one all-gather
              of the per-level partials and the exact combine on every rank
@@ -29,6 +40,8 @@ cpu_baseline the oracle's restatement of the reference's chunk loop on this
 import argparse
 import json
 import os
+import platform
+import re
 import subprocess
 import sys
 import threading
@@ -42,6 +55,10 @@ WORKLOAD = "D(1e20) hard special leaves, Gourdon default parameters (y=z=2455353
 METRIC = "pi(1e20) sec & hard-leaves/s on 1 GB300"
 UNIT = "hard-leaves/s"
 TOTAL_LEAVES_1E20 = 22178370075
+# hard leaves of D(x) at the reference's default parameters (deterministic;
+# the engine's and the oracle's counts agree)
+LEAVES = {10 ** 20: TOTAL_LEAVES_1E20}
+REF_BIN = os.path.join(ROOT, "oracle", "_ref", platform.machine(), "primecount")
 
 
 def clocks_sampler(stop, out):
@@ -90,15 +107,18 @@ def measured_peaks():
 
 
 def profile_traffic():
-    """DRAM bytes per k_sweep launch of D(1e20), from the committed summary
-    of the ncu capture (its line `dram_bytes_per_launch: N`), if present."""
-    p = os.path.join(ROOT, "profiles", "k_sweep_traffic_D1e20.md")
+    """DRAM bytes per algorithmic byte of k_sweep, from the committed summary
+    of an ncu capture of every k_sweep launch of a smaller D (its line
+    `dram_bytes_per_alg_byte: R`), if present; scaled to a launch of this
+    workload by its algorithmic bytes."""
+    p = os.path.join(ROOT, "profiles", "k_sweep_traffic_D1e18.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
-        if line.strip().startswith("dram_bytes_per_launch:"):
+        if line.strip().startswith("dram_bytes_per_alg_byte:"):
             try:
-                return {"dram_bytes_per_launch": float(line.split(":", 1)[1].strip().split()[0])}
+                return {"ratio": float(line.split(":", 1)[1].strip().split()[0]),
+                        "source": "profiles/k_sweep_traffic_D1e18.md"}
             except ValueError:
                 return None
     return None
@@ -120,35 +140,68 @@ def profile_issue():
     return None
 
 
+def ref_D(x, threads):
+    """(D(x), seconds) from the reference's own CLI: `primecount x --D -t N
+    --time` (src/app/main.cpp:205-246, 569-570), the time being the
+    reference's get_time() around its D()."""
+    out = subprocess.run([REF_BIN, str(x), "--D", "-t%d" % threads, "--time"], check=True, capture_output=True,
+                         text=True).stdout
+    val = int(out.strip().splitlines()[0])
+    secs = float(re.search(r"Seconds:\s*([0-9.]+)", out).group(1))
+    return val, secs
+
+
+def ref_build_flags():
+    p = os.path.join(os.path.dirname(REF_BIN), "build_flags.txt")
+    try:
+        return open(p).read().strip()
+    except OSError:
+        return None
+
+
 def cpu_baseline(p, threads, target_s=12.0):
+    """The reference's own D(x) over the whole workload on all host threads
+    (kind "reference"), or, without the reference build, the oracle's
+    restatement of its chunk loop on a sample of the interval (kind "port")."""
+    why = "the reference's build is missing"
+    if os.access(REF_BIN, os.X_OK) and X in LEAVES:
+        try:
+            val, secs = ref_D(X, threads)
+            return {"value": LEAVES[X] / secs, "unit": UNIT, "cores": threads, "kind": "reference",
+                    "sample": "the whole D(%s) (%d hard leaves) by the reference's own --D on %d threads: %.2f s, "
+                              "result %d" % (args_x_str(), LEAVES[X], threads, secs, val),
+                    "seconds": secs, "build": ref_build_flags()}
+        except (subprocess.CalledProcessError, OSError, AttributeError, ValueError) as e:
+            why = "the reference's build failed to run: %s" % str(e)[:200]
+    r = port_sample(p, threads, target_s)
+    r["why_port"] = why
+    return r
+
+
+def args_x_str():
+    return "%.0e" % X if X >= 10 ** 6 else str(X)
+
+
+def port_sample(p, threads, target_s=12.0):
     """Oracle restatement of the reference's chunk loop, timed on a sample of
-    D(1e20): nchunks sub-intervals starting at c / nchunks of [0, x/z), all
-    host threads.  The rate is the sample's leaves over its wall time (the
-    metric's unit); the sample fraction grows until it takes about target_s
-    (at most 10x per step while it is tiny; then by the 4th root of the
-    remaining factor: its cost grows much faster than the fraction, the
-    leaves being densest near 0)."""
+    D(x): nchunks sub-intervals starting at c / nchunks of [0, x/z), all
+    host threads.  The rate is the sample's leaves over its wall time; the
+    sample fraction grows until it takes about target_s."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.load()
     nchunks = max(64, 4 * threads)
     frac = 1e-4
     leaves, secs = oracle.D_sample(X, p["y"], p["z"], p["k"], nchunks, frac, threads)
-    spent = secs
     while secs < target_s * 2 / 3 and frac < 0.05:
-        # the sample's cost grows about as its fraction to the 4th power once
-        # the first sub-interval reaches the dense start of the interval
         step = min(10.0, 0.8 * target_s / max(secs, 1e-3)) if secs < 0.3 else \
             max(1.1, min(2.0, (target_s / secs) ** 0.25))
         frac = min(0.05, frac * step)
         leaves, secs = oracle.D_sample(X, p["y"], p["z"], p["k"], nchunks, frac, threads)
-        spent += secs
-    rate = leaves / secs
-    return {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "oracle chunk loop on %d sub-intervals starting at c/%d of [0, x/z) of D(1e20), "
-                      "together %.4g of the interval: %d leaves (%.1f%% of D's) in %.1f s wall on %d threads"
-                      % (nchunks, nchunks, frac, leaves, 100.0 * leaves / TOTAL_LEAVES_1E20, secs, threads),
-            "sample_seconds": secs, "calibration_seconds": spent}
+    return {"value": leaves / secs, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "oracle chunk loop (the reference's build is missing) on %d sub-intervals starting at "
+                      "c/%d of [0, x/z), together %.4g of the interval: %d leaves in %.1f s wall on %d threads"
+                      % (nchunks, nchunks, frac, leaves, secs, threads)}
 
 
 def batch_workload(n, seed=20261203):
@@ -207,26 +260,60 @@ def run_batch(args, pcg):
 
 
 def run_reference(args, rank):
+    """The reference's own D(x) (its CLI, OpenMP on all host threads): one
+    whole evaluation per timed step.  Nothing of primecount_gb300 is
+    imported: the reference's defaults give y, z, k itself."""
     if rank != 0:
         return
-    import primecount_gb300 as pcg
-    p = pcg.gourdon_params(X)
     threads = os.cpu_count() or 1
-    vals = []
-    for _ in range(args.warmup):
-        pass
-    t0 = time.time()
+    base = {"impl": "reference", "metric": METRIC, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int64/int128", "data": "synthetic (scalar x)",
+            "config": {"workload": WORKLOAD if X == 10 ** 20 else "D(%s)" % args.x, "x": args.x,
+                       "l2": "n/a (CPU)"}}
+    why = None
+    if not os.access(REF_BIN, os.X_OK) or X not in LEAVES:
+        why = "the reference's build is missing"
+    else:
+        try:
+            for _ in range(max(1, args.warmup)):
+                ref_D(X // 1000, threads)
+        except (subprocess.CalledProcessError, OSError, AttributeError, ValueError) as e:
+            why = "the reference's build failed to run: %s" % str(e)[:200]
+    if why:
+        # the reference did not build on this host: the oracle's restatement
+        p = None
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        oracle.load()
+        p = oracle.gourdon_params(X)
+        vals, t0 = [], time.time()
+        for _ in range(args.steps):
+            cb = port_sample(p, threads, target_s=8.0)
+            vals.append(cb["value"])
+        v = sum(vals) / len(vals)
+        line = dict(base, value=v, ms_per_step=1000 * (time.time() - t0) / max(args.steps, 1),
+                    cpu_baseline={"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                  "sample": cb["sample"], "why_port": why},
+                    e2e={"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0})
+        print(json.dumps(line), flush=True)
+        return
+    secs, wall, val = [], [], None
     for _ in range(args.steps):
-        cb = cpu_baseline(p, threads, target_s=8.0)
-        vals.append(cb["value"])
-    dt = time.time() - t0
-    v = sum(vals) / len(vals)
-    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / max(args.steps, 1),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64/int128",
-            "data": "synthetic (scalar x)", "config": {"workload": WORKLOAD, "x": "1e20", "l2": "n/a (CPU)"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": cb["sample"]},
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        t0 = time.perf_counter()
+        val, s_ = ref_D(X, threads)
+        wall.append(time.perf_counter() - t0)
+        secs.append(s_)
+    ms = 1000.0 * sum(secs) / len(secs)
+    v = LEAVES[X] / (ms / 1000.0)
+    line = dict(base, value=v, ms_per_step=ms, result=str(val),
+                cpu_baseline={"value": v, "unit": UNIT, "cores": threads, "kind": "reference",
+                              "sample": "the whole D(%s) per step (%d hard leaves) by the reference's own --D "
+                                        "on %d threads; warm-up steps (at least one) D(x/1000)"
+                                        % (args.x, LEAVES[X], threads),
+                              "build": ref_build_flags(), "step_seconds": secs,
+                              "step_wall_seconds": wall},
+                e2e={"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0})
     print(json.dumps(line), flush=True)
 
 
@@ -384,19 +471,40 @@ def main():
     if rank != 0:
         return
     peak, peak_kind = measured_peaks()
-    # 2 B per FactorTableD entry read, 4 B per two-prime leaf (its prime),
-    # 8 B per leaf (the reciprocal of m or of the prime), 16 B per
-    # (segment, level) step (PiTable word of the level bounds)
-    alg_bytes = 2 * st["factor_entries"] + 4 * st["two_prime_leaves"] + 8 * st["leaves"] + 16 * st["levels"]
+    # algorithmic bytes of the hot-path table: 2 B per FactorTableD entry
+    # read, 4 B per two-prime leaf (its prime), 16 B per (segment, level)
+    # step (PiTable word of the level bounds); the 8 B reciprocal of m (or of
+    # the prime) per leaf is this implementation's own traffic
+    alg_bytes = 2 * st["factor_entries"] + 4 * st["two_prime_leaves"] + 16 * st["levels"]
+    impl_bytes = 8 * st["leaves"]
     k_ms_call = kernel_ms / args.steps
     launches_call = launches / args.steps
-    achieved = alg_bytes / (k_ms_call / 1000.0) / 1e9
+    launch_s = k_ms_call / launches_call / 1000.0
+    achieved = alg_bytes / launches_call / launch_s / 1e9
     tr = profile_traffic()
-    traffic = tr["dram_bytes_per_launch"] if tr else None
+    traffic = tr["ratio"] * alg_bytes / launches_call if tr else None
+    # algorithmic integer / shared-memory operations: per leaf one division
+    # and one prefix query (a counter load and up to 8 popcounts), per
+    # cross-off multiple one shared-memory read-modify-write; against the
+    # lane issue rate of the SMs (SMs x 128 lanes x SM clock)
+    clk = summarize_clocks(rows, torch.cuda.current_device())
+    sm_mhz = clk["sm_mhz"] or 2070.0
+    nsm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    ops = 10 * st["leaves"] + st["crossoff_multiples"]
+    ops_peak = nsm * 128 * sm_mhz * 1e6
+    ops_achieved = ops / launches_call / launch_s
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
             "kernel": "k_sweep", "alg_bytes_per_launch": alg_bytes / launches_call,
+            "impl_bytes_per_launch": impl_bytes / launches_call,
+            "impl_achieved_gbs": (alg_bytes + impl_bytes) / launches_call / launch_s / 1e9,
+            "traffic_source": tr["source"] if tr else None,
             "launch_ms": k_ms_call / launches_call, "launches_per_step": launches_call,
+            "int_ops": {"ops_per_launch": ops / launches_call, "ops_per_leaf": ops / max(st["leaves"], 1),
+                        "crossoff_multiples_per_step": st["crossoff_multiples"],
+                        "achieved_gops": ops_achieved / 1e9, "peak_gops": ops_peak / 1e9,
+                        "frac": ops_achieved / ops_peak,
+                        "peak": "%d SMs x 128 lanes x %.0f MHz (lane issue rate)" % (nsm, sm_mhz)},
             "issue_active": profile_issue()}
     cpu = None
     if not args.no_cpu and X == 10 ** 20:
@@ -415,7 +523,7 @@ def main():
             "serve": serve,
             "gpu_launches": int(st["kernel_launches"]) * args.steps,
             "roofline": roof, "cpu_baseline": cpu,
-            "clocks": summarize_clocks(rows, torch.cuda.current_device()),
+            "clocks": clk,
             "wall_s": wall}
     print(json.dumps(line), flush=True)
 

@@ -103,6 +103,8 @@ typedef struct {
   int ctas_per_sm;
   int threads_per_cta;
   double ac_ms, b_ms, phi0_ms, sigma_ms, d_ms; /* pi(x): time of each Gourdon term   */
+  uint64_t crossoff_multiples; /* multiples of the sieving primes crossed off in the
+                                  segments (the sieve's shared-memory updates)      */
 } pcg_stats;
 
 /* ---- contexts: device-resident prime / PiTable / FactorTable state ---- */
@@ -118,6 +120,29 @@ const char* pcg_last_error(const pcg_ctx* ctx);
 pcg_status pcg_last_stats(const pcg_ctx* ctx, pcg_stats* out);
 /* Device bytes held by the context's resident tables. */
 uint64_t pcg_ctx_device_bytes(const pcg_ctx* ctx);
+
+/* Resident tables of a context, for inspection and table-level tests (no
+ * counterpart in the reference, whose tables are local objects of each
+ * call; its own tests check them entry by entry, test/gourdon/
+ * FactorTableD.cpp, test/lmo/FactorTable.cpp, test/PiTable.cpp).  Entry
+ * formats are the reference's:
+ *   PCG_TABLE_PRIMES     uint32, primes[0] = 0, primes[1..] = 2, 3, 5, ...
+ *                        (PiTable::get_primes, src/PiTable.hpp)
+ *   PCG_TABLE_PI         uint64 pairs {count, bits} per 240 numbers (src/PiTable.cpp)
+ *   PCG_TABLE_FACTOR_D   FactorTableD entries, 2 or 4 bytes (src/gourdon/FactorTableD.hpp)
+ *   PCG_TABLE_FACTOR_DR  FactorTable entries, 2 or 4 bytes (src/FactorTable.hpp) */
+enum {
+  PCG_TABLE_PRIMES = 0,
+  PCG_TABLE_PI = 1,
+  PCG_TABLE_FACTOR_D = 2,
+  PCG_TABLE_FACTOR_DR = 3
+};
+/* Copies entries [first, first + count) of a resident table to the host
+ * buffer out (count * entry size bytes) and writes the table's number of
+ * entries, entry size in bytes and the largest number it covers (0 / -1
+ * when the table is not built yet).  count = 0 only reports the sizes. */
+pcg_status pcg_ctx_read_table(const pcg_ctx* ctx, int table, uint64_t first, uint64_t count, void* out,
+                              uint64_t* entries, int* entry_bytes, int64_t* limit);
 
 /* ---- the hard-leaf formulas ---- */
 
@@ -156,19 +181,22 @@ pcg_status pcg_shard_combine(int nshards, int64_t cols, const pcg_i128* acc, con
 
 /* D(x, y, z, k) without allocating device memory.  No counterpart in the
  * reference.  For callers that cannot call cudaMalloc when they need the
- * result: code running while a stream is being captured into a CUDA graph,
- * request paths of a serving loop that must not touch the allocator, or
- * processes whose device memory belongs to another framework's pool.  The
- * tables are inputs: ctx must have been created (pcg_ctx_create, which does
- * allocate, at set-up time) with a max_x whose tables cover y and z, else
- * PCG_ERANGE.  All working memory comes from one 64 MiB static device array
- * that every GPU loading the library holds until exit; a call needing more
- * (or more than 32768 levels) is rejected with PCG_ERANGE.  The first call on
- * a device looks up the array's device address, so make it before any stream
- * capture.  Calls share the array and it keeps the last call's contents
- * (what must start at zero is cleared on the stream); calls overlapping on
- * the GPU race, so run them on one stream or one after another.  stream may
- * be NULL (the context's stream); the result is written to *out on return. */
+ * result: request paths of a serving loop that must not touch the
+ * allocator, or processes whose device memory belongs to another
+ * framework's pool (where a cudaMalloc fails or takes memory the pool
+ * accounts for).  The tables are inputs: ctx must have been created
+ * (pcg_ctx_create, which does allocate, at set-up time) with a max_x whose
+ * tables cover y and z, else PCG_ERANGE.  All device working memory comes
+ * from one 64 MiB static device array that every GPU loading the library
+ * holds until exit; a call needing more (or more than 32768 levels) is
+ * rejected with PCG_ERANGE.  The call runs on ctx's device.  The first call
+ * on a device looks up the array's device address (cudaGetSymbolAddress),
+ * so make that first call before any stream capture.  Calls share the array
+ * and it keeps the last call's contents (what must start at zero is cleared
+ * on the stream); calls run one at a time on the host and each waits for
+ * its own work before returning, but calls whose work overlaps on the GPU
+ * race on the array.  stream may be NULL (the context's stream); the result
+ * is written to *out on return. */
 pcg_status pcg_D_noalloc(pcg_ctx* ctx, pcg_i128 x, int64_t y, int64_t z, int64_t k,
                          void* stream, pcg_i128* out);
 

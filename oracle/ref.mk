@@ -1,33 +1,87 @@
-# Compiles the reference primecount (CPU, OpenMP) from its own sources, where
-# they lie, into oracle/_ref/.  This is test infrastructure: the binary is the
-# checker used to generate golden fixtures and to validate the C restatement in
-# oracle/pcg_oracle.c.  Nothing in the product links it.
+# Compiles the reference primecount (CPU, OpenMP) from its own sources into
+# oracle/_ref/.  This is test infrastructure: the binary is the checker used to
+# generate golden fixtures, to validate the C restatement in
+# oracle/pcg_oracle.c, and the timed CPU reference of bench.py.  Nothing in
+# the product links it.
 #
-#   make -f oracle/ref.mk REF=/root/reference -j8
+#   make -f oracle/ref.mk REF=<primecount source tree> -j8       # build
+#   make -f oracle/ref.mk REF=<primecount source tree> stage      # see below
 #
-# Output: oracle/_ref/primecount (CLI) and oracle/_ref/libprimecount_ref.a
-REF    ?= /root/reference
-OUT    ?= oracle/_ref
+# REF defaults to $(PCG_REFERENCE).  The flags follow the reference's CMake
+# Release build: -O3, OpenMP, libdivide, int128, and its run-time CPU
+# dispatch (ENABLE_MULTIARCH_*) where the compiler supports the target
+# attribute -- AVX512 VPOPCNTDQ on x86-64, SVE on aarch64 (the reference's
+# cmake/multiarch_*.cmake decide the same way; SVE also needs a host CPU
+# that reports it, see below).
+#
+# `stage` copies the source files this recipe compiles into $(STAGE) (a
+# git-ignored directory, never committed), so that a host without the
+# reference tree (the aarch64 GPU host) can build the reference with
+# REF=$(STAGE).
+#
+# Output: $(OUT)/primecount (CLI) and $(OUT)/libprimecount_ref.a, one
+# directory per CPU architecture.
+REF    ?= $(PCG_REFERENCE)
+ARCH   := $(shell uname -m)
+OUT    ?= oracle/_ref/$(ARCH)
+STAGE  ?= oracle/_ref/src
 CXX    ?= g++
-CXXFLAGS ?= -O2 -std=gnu++17 -fopenmp -DNDEBUG
-INC    := -I$(REF)/include -I$(REF)/src -I$(REF)/lib/primesieve/include
+HERE   := $(dir $(lastword $(MAKEFILE_LIST)))
+
+ifeq ($(strip $(REF)),)
+$(error set REF=<primecount source tree> or PCG_REFERENCE)
+endif
+
+CXXFLAGS ?= -O3 -std=gnu++17 -fopenmp -DNDEBUG
+DEFS   := -DENABLE_LIBDIVIDE
+PS_DEFS :=
+ARCH_SRC :=
+PS_ARCH_SRC :=
+
+# run-time dispatch: only when the compiler accepts the probe
+ifeq ($(ARCH),x86_64)
+ifeq ($(shell $(CXX) -std=gnu++17 -c -x c++ $(HERE)probe_avx512.cpp -o /dev/null 2>/dev/null && echo 1),1)
+DEFS    += -DENABLE_MULTIARCH_x86_POPCNT -DENABLE_MULTIARCH_AVX512_VPOPCNT
+PS_DEFS += -DENABLE_MULTIARCH_x86_POPCNT -DENABLE_MULTIARCH_AVX512_BW -DENABLE_MULTIARCH_AVX512_VBMI2
+ARCH_SRC := $(REF)/src/arch/x86/cpuid.cpp
+PS_ARCH_SRC := $(REF)/lib/primesieve/src/arch/x86/cpuid.cpp
+endif
+endif
+# aarch64: SVE dispatch only where the host's CPU reports SVE (the Grace cores
+# of the GB300 host do not expose it, and a build with SVE dispatch compiled
+# in died there with SIGILL; without it the reference runs its default path)
+SVE_HOST := $(shell grep -qw sve /proc/cpuinfo 2>/dev/null && echo 1)
+ifeq ($(ARCH)$(SVE_HOST),aarch641)
+ifeq ($(shell $(CXX) -std=gnu++17 -c -x c++ $(HERE)probe_sve.cpp -o /dev/null 2>/dev/null && echo 1),1)
+DEFS    += -DENABLE_MULTIARCH_ARM_SVE
+PS_DEFS += -DENABLE_MULTIARCH_ARM_SVE
+ARCH_SRC := $(REF)/src/arch/arm/sve.cpp
+PS_ARCH_SRC := $(REF)/lib/primesieve/src/arch/arm/sve.cpp
+endif
+endif
+
+INC    := -I$(REF)/include -I$(REF)/src -I$(REF)/lib/primesieve/include -I$(REF)/lib/primesieve/src
 
 PC_SRC := $(filter-out $(REF)/src/app/%,$(wildcard $(REF)/src/*.cpp) \
           $(REF)/src/sieve/Sieve.cpp $(REF)/src/sieve/pre_sieve.cpp \
           $(wildcard $(REF)/src/lmo/*.cpp) $(wildcard $(REF)/src/deleglise-rivat/*.cpp) \
-          $(wildcard $(REF)/src/gourdon/*.cpp))
-PS_SRC := $(wildcard $(REF)/lib/primesieve/src/*.cpp)
+          $(wildcard $(REF)/src/gourdon/*.cpp)) $(ARCH_SRC)
+PS_SRC := $(wildcard $(REF)/lib/primesieve/src/*.cpp) $(PS_ARCH_SRC)
 APP_SRC := $(wildcard $(REF)/src/app/*.cpp)
 
 PC_OBJ := $(patsubst $(REF)/%.cpp,$(OUT)/obj/%.o,$(PC_SRC))
 PS_OBJ := $(patsubst $(REF)/%.cpp,$(OUT)/obj/%.o,$(PS_SRC))
 APP_OBJ := $(patsubst $(REF)/%.cpp,$(OUT)/obj/%.o,$(APP_SRC))
 
-all: $(OUT)/primecount $(OUT)/libprimecount_ref.a
+all: $(OUT)/primecount $(OUT)/libprimecount_ref.a $(OUT)/build_flags.txt
 
-$(OUT)/obj/%.o: $(REF)/%.cpp
+$(OUT)/obj/lib/primesieve/%.o: $(REF)/lib/primesieve/%.cpp
 	@mkdir -p $(dir $@)
-	$(CXX) $(CXXFLAGS) $(INC) -c $< -o $@
+	$(CXX) $(CXXFLAGS) $(PS_DEFS) $(INC) -c $< -o $@
+
+$(OUT)/obj/src/%.o: $(REF)/src/%.cpp
+	@mkdir -p $(dir $@)
+	$(CXX) $(CXXFLAGS) $(DEFS) $(INC) -c $< -o $@
 
 $(OUT)/libprimecount_ref.a: $(PC_OBJ) $(PS_OBJ)
 	ar rcs $@ $^
@@ -35,4 +89,12 @@ $(OUT)/libprimecount_ref.a: $(PC_OBJ) $(PS_OBJ)
 $(OUT)/primecount: $(APP_OBJ) $(OUT)/libprimecount_ref.a
 	$(CXX) $(CXXFLAGS) $(APP_OBJ) $(OUT)/libprimecount_ref.a -o $@
 
-.PHONY: all
+$(OUT)/build_flags.txt: $(OUT)/primecount
+	@echo "arch=$(ARCH) cxx=$$($(CXX) -dumpfullversion) flags=$(CXXFLAGS) defs=$(DEFS) primesieve_defs=$(PS_DEFS)" > $@
+
+# the sources compiled above plus the headers they include
+stage:
+	@mkdir -p $(STAGE)
+	cd $(REF) && cp -r --parents include src lib/primesieve/include lib/primesieve/src COPYING $(abspath $(STAGE))/
+
+.PHONY: all stage

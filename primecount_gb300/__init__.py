@@ -61,7 +61,8 @@ class Stats(ctypes.Structure):
                 ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
                 ("segment_words", ctypes.c_int), ("ctas_per_sm", ctypes.c_int),
                 ("threads_per_cta", ctypes.c_int), ("ac_ms", ctypes.c_double), ("b_ms", ctypes.c_double),
-                ("phi0_ms", ctypes.c_double), ("sigma_ms", ctypes.c_double), ("d_ms", ctypes.c_double)]
+                ("phi0_ms", ctypes.c_double), ("sigma_ms", ctypes.c_double), ("d_ms", ctypes.c_double),
+                ("crossoff_multiples", ctypes.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -121,6 +122,9 @@ def load(path=None):
     L.pcg_D_shard.argtypes = shard_args
     L.pcg_S2_hard_shard.argtypes = shard_args
     L.pcg_shard_combine.argtypes = [ctypes.c_int, c_i64, c_p(I128), c_p(c_i64), c_p(c_i64), c_p(I128)]
+    L.pcg_ctx_read_table.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64,
+                                     ctypes.c_void_p, c_p(ctypes.c_uint64), c_p(ctypes.c_int), c_p(c_i64)]
+    L.pcg_ctx_read_table.restype = ctypes.c_int
     L.pcg_autotune.argtypes = [I128, c_p(Opts), c_p(Tuning)]
     L.pcg_autotune.restype = ctypes.c_int
     for name in ("pcg_D", "pcg_S2_hard", "pcg_D_default", "pcg_S2_hard_default", "pcg_gourdon_params",
@@ -168,6 +172,28 @@ class Context:
         s = Stats()
         _check(load().pcg_last_stats(self._h, ctypes.byref(s)), self)
         return s.as_dict()
+
+    TABLES = {"primes": 0, "pi": 1, "factor_d": 2, "factor_dr": 3}
+
+    def table_info(self, name):
+        """(entries, entry bytes, largest number covered) of a resident table."""
+        n, eb, lim = ctypes.c_uint64(), ctypes.c_int(), ctypes.c_int64()
+        _check(load().pcg_ctx_read_table(self._h, self.TABLES[name], 0, 0, None, ctypes.byref(n), ctypes.byref(eb),
+                                         ctypes.byref(lim)), self)
+        return n.value, eb.value, lim.value
+
+    def read_table(self, name, first=0, count=None):
+        """Entries [first, first + count) of a resident table as a numpy array
+        (pcg_ctx_read_table): "primes", "pi", "factor_d" or "factor_dr"."""
+        import numpy as np
+        n, eb, _ = self.table_info(name)
+        if count is None:
+            count = n - first
+        arr = np.empty(count, dtype={2: np.uint16, 4: np.uint32, 8: np.uint64}[eb])
+        if count:
+            _check(load().pcg_ctx_read_table(self._h, self.TABLES[name], first, count, arr.ctypes.data_as(ctypes.c_void_p),
+                                             None, None, None), self)
+        return arr
 
 
 def _opts(ctx=None, stream=None, threads=0, print_=False, segment_words=0, ctas_per_sm=0, cta_threads=0,

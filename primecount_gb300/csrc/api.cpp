@@ -587,6 +587,57 @@ pcg_status pcg_D_noalloc(pcg_ctx* ctx, pcg_i128 xi, int64_t y, int64_t z, int64_
   });
 }
 
+pcg_status pcg_ctx_read_table(const pcg_ctx* ctx, int table, uint64_t first, uint64_t count, void* out,
+                              uint64_t* entries, int* entry_bytes, int64_t* limit)
+{
+  if (!ctx) return PCG_EINVAL;
+  Ctx* cp = (Ctx*) ctx;
+  return guard(cp, [&] {
+    std::lock_guard<std::recursive_mutex> lk(cp->call_mu);
+    const Tables& t = cp->tab;
+    const DevBuf* buf = nullptr;
+    uint64_t n = 0;
+    int eb = 0;
+    int64_t lim = -1;
+    switch (table) {
+      case PCG_TABLE_PRIMES:
+        if (t.prime_limit >= 0) { buf = &t.primes; n = (uint64_t) t.nprimes + 1; eb = 4; lim = t.prime_limit; }
+        break;
+      case PCG_TABLE_PI:
+        if (t.prime_limit >= 0) { buf = &t.pitab; n = 2 * (uint64_t) (t.prime_limit / 240 + 1); eb = 8; lim = t.prime_limit; }
+        break;
+      case PCG_TABLE_FACTOR_D:
+        if (t.fd_z >= 0) {
+          buf = &t.factor_d;
+          n = (uint64_t) wheel2310().to_index((uint64_t) std::max<int64_t>(t.fd_z, 1)) + 1;
+          eb = t.fd_bytes;
+          lim = t.fd_z;
+        }
+        break;
+      case PCG_TABLE_FACTOR_DR:
+        if (t.fr_y >= 0) {
+          buf = &t.factor_dr;
+          n = (uint64_t) wheel2310().to_index((uint64_t) std::max<int64_t>(t.fr_y, 1)) + 1;
+          eb = t.fr_bytes;
+          lim = t.fr_y;
+        }
+        break;
+      default:
+        fail(PCG_EINVAL, "unknown table " + std::to_string(table));
+    }
+    if (entries) *entries = n;
+    if (entry_bytes) *entry_bytes = eb;
+    if (limit) *limit = lim;
+    if (count == 0) return;
+    if (!buf || !out) fail(PCG_EINVAL, "the table is not resident or out is NULL");
+    if (first > n || count > n - first) fail(PCG_ERANGE, "entries beyond the table");
+    PCG_CUDA(cudaSetDevice(cp->device));
+    PCG_CUDA(cudaStreamSynchronize(cp->stream));
+    PCG_CUDA(cudaMemcpy(out, (const char*) buf->p + first * (uint64_t) eb, count * (uint64_t) eb,
+                        cudaMemcpyDeviceToHost));
+  });
+}
+
 pcg_status pcg_D_default(pcg_i128 xi, const pcg_opts* opts, pcg_i128* out, int64_t* y, int64_t* z, int64_t* k)
 {
   int64_t yy = 1, zz = 1, kk = 0, xs = 0;

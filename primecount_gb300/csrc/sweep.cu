@@ -335,7 +335,8 @@ struct SweepArgs {
   uint32_t* cnt;            // [wave_len][bglob+1]
   int32_t* smu;             // [wave_len][bglob+1]
   int64_t* segsum;          // [wave_len]
-  unsigned long long* counters;  // [0] leaves, [1] two-prime leaves, [2] levels, [3] factor entries
+  unsigned long long* counters;  // [0] leaves, [1] two-prime leaves, [2] levels, [3] factor entries,
+                                 // [4] multiples crossed off
   int* queue;
   int group_max;            // levels answered together (<= GROUP_MAX; < 2: off)
 };
@@ -494,7 +495,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
   __shared__ long long wt3[32][3];
   __shared__ int s_brk[32];
   __shared__ long long s_red[NT / 32];
-  __shared__ unsigned long long s_ctr[4];
+  __shared__ unsigned long long s_ctr[5];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const u128 x = ((u128) A.x_hi << 64) | A.x_lo;
@@ -516,7 +517,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
     }
     pat[i] = w;
   }
-  if (tid < 4) s_ctr[tid] = 0;
+  if (tid < 5) s_ctr[tid] = 0;
 
   for (;;) {
     __syncthreads();
@@ -590,6 +591,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
         LevelP P;
         P.lo = P.hi = 0; P.jlo = 0; P.jn = 0; P.prime = 0; P.thr = 0; P.flags = 0; P.level = b; P.fcount = 0;
         uint32_t pcv = 0;
+        uint32_t ncross = 0;   // multiples of p_b in the segment (work counter)
         if (b <= Bs) {
           const uint64_t p = A.primes[b];
           P.prime = (uint32_t) p;
@@ -616,7 +618,13 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
           } else if (p >= 7) {
             P.jlo = (uint64_t) ((low / 240) % p);   // pattern phase of the first word
             P.flags |= 4;
+            // its multiples in the segment, for the work counter only
+            uint64_t qlo = ((uint64_t) low + p - 1) / p;
+            if (qlo < 1) qlo = 1;
+            const uint64_t qhi = ((uint64_t) high - 1) / p;
+            if (qlo <= qhi) ncross = (uint32_t) (cnt_le(qhi) - cnt_le(qlo - 1));
           }
+          if (p >= 64) ncross = P.jn;
           if (b >= bmin_leaf && b <= bmax_leaf) {
             const uint64_t* xt = A.xp_tab + 3 * b;
             const u128 xp = ((u128) xt[1] << 64) | xt[0];
@@ -679,6 +687,8 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
         fcnt = P.fcount;
         lp[tid] = P;
         s_pc[tid] = pcv;
+        ncross = __reduce_add_sync(0xffffffffu, ncross);
+        if (lane == 0 && ncross) atomicAdd(&s_ctr[4], (unsigned long long) ncross);
       }
       __syncthreads();
       const int nb = (int) dmin(NT, (int64_t) (Bs - b0 + 1));
@@ -1265,7 +1275,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
     }
   }
   __syncthreads();
-  if (tid < 4 && s_ctr[tid]) atomicAdd(&A.counters[tid], s_ctr[tid]);
+  if (tid < 5 && s_ctr[tid]) atomicAdd(&A.counters[tid], s_ctr[tid]);
 }
 
 // ---- phi offsets: acc[b] += sum_s M(s, b) * sum_{s'<s} C(s', b), in segment order.
@@ -1580,10 +1590,14 @@ void ensure_factor_d(Ctx& c, int64_t y, int64_t z, cudaStream_t s)
   Tables& t = c.tab;
   bool ok = t.fd_z >= z && (t.fd_y == y || (y >= z && t.fd_y >= z));
   if (ok) return;
-  if (z > 386083ll * 386083 - 1 && false) fail(PCG_ERANGE, "z too large");
   double t0 = now_ms();
   ensure_prime_tables(c, std::max<int64_t>(y, isqrt((u128) z) + 1), s);
-  t.fd_bytes = (z <= 386083ll * 386083 - 1) ? 2 : 4;
+  // 16-bit entries whenever possible, as the reference's D() chooses
+  // (src/gourdon/D.cpp:477-499); PCG_FACTOR_D_U32=1 forces the 32-bit table,
+  // whose size limit no practical z reaches, so that it can be tested
+  const char* f32 = getenv("PCG_FACTOR_D_U32");
+  const bool force32 = f32 && atoi(f32) == 1;
+  t.fd_bytes = (z <= 386083ll * 386083 - 1 && !force32) ? 2 : 4;
   if (t.fd_bytes == 2) build_factor<uint16_t>(c, t.factor_d, z, y, 1, s);
   else build_factor<uint32_t>(c, t.factor_d, z, y, 1, s);
   ensure_finv(c, wheel2310().to_index((uint64_t) std::max<int64_t>(z, 1)) + 1, s);
@@ -1636,28 +1650,30 @@ static void launch_sweep(const SweepArgs& a, int grid, size_t smem, cudaStream_t
 // of square-free numbers without prime factors <= p_b, or the prime density
 // for the p_b * p_l leaves) plus a per-level cost, integrated on a geometric
 // grid; segments are cut at equal estimated cost, never longer than smax.
-static std::vector<int64_t> plan_segments(const SweepProblem& pb, const Tables& t, int64_t L, int64_t x_star,
-                                          int64_t pi_sqrt, int64_t bglob, int64_t smax, int grid)
+// dens[b] = 0.56 / log(p_b) for b in [1, bglob].  The grid cells are costed
+// on nth host threads (1: the calling thread only, no thread is created).
+// Each segment end is passed to push(end) in order, starting with 0; a push
+// returning false stops the plan (the return value is then false).
+#define PLAN_GRID 1200
+template <class Push>
+static bool plan_segments_core(const SweepProblem& pb, const Tables& t, int64_t L, int64_t x_star,
+                               int64_t pi_sqrt, int64_t bglob, int64_t smax, int grid, const double* dens,
+                               unsigned nth, Push push)
 {
   const double x = (double) pb.x;
   const double y = (double) pb.y, z = (double) pb.z;
-  const int G = 1200;
-  std::vector<double> g;
-  g.push_back(0);
-  double a0 = 240;
-  double ratio = std::pow((double) L / a0, 1.0 / (G - 1));
-  for (int i = 0; i < G; i++) g.push_back(std::min((double) L, a0 * std::pow(ratio, i)));
-  g.back() = (double) L;
-  std::vector<double> pr((size_t) bglob + 1), dens((size_t) bglob + 1);
-  for (int64_t b = 1; b <= bglob; b++) {
-    pr[b] = (double) t.h_primes[(size_t) b];
-    dens[b] = 0.56 / std::log(std::max(pr[b], 3.0));
-  }
+  const int G = PLAN_GRID;
+  double g[G + 1], cost[G], cum[G + 1];
+  g[0] = 0;
+  const double a0 = 240;
+  const double ratio = std::pow((double) L / a0, 1.0 / (G - 1));
+  for (int i = 0; i < G; i++) g[i + 1] = std::min((double) L, a0 * std::pow(ratio, i));
+  g[G] = (double) L;
   auto leaves = [&](double lo, double hi) {
     double sum = 0;
     double l1 = std::max(lo, 1.0);
     for (int64_t b = pb.k + 1; b <= bglob; b++) {
-      const double p = pr[b], xp = x / p;
+      const double p = (double) t.h_primes[(size_t) b], xp = x / p;
       double mlo, mhi;
       if (pb.gourdon == 2) { mlo = std::max(y / p, xp / hi); mhi = std::min(xp / l1, y); }
       else if (pb.gourdon) {
@@ -1675,58 +1691,69 @@ static std::vector<int64_t> plan_segments(const SweepProblem& pb, const Tables& 
   auto levels = [&](double a) {
     double lim = pb.gourdon ? std::min((double) x_star, std::sqrt(x / std::max(a, 1.0)))
                             : std::min(std::sqrt(z), std::sqrt(x / std::max(a, 1.0)));
-    if (pb.gourdon == 2) lim = std::min((double) x_star, std::sqrt(x / std::max(a, 1.0)));
     return (double) host_pi(t, (uint64_t) std::min(lim, (double) t.prime_limit));
   };
   const double c_level = 30.0;
-  // the cost of each grid cell, the cells spread over the host threads
-  const size_t ncell = g.size() - 1;
-  std::vector<double> cost(ncell, 0.0);
-  {
-    const unsigned nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  auto cell = [&](unsigned k, unsigned step) {
+    for (int i = (int) k; i < G; i += (int) step) {
+      const double len = g[i + 1] - g[i];
+      cost[i] = len > 0 ? leaves(g[i], g[i + 1]) + c_level * levels(g[i]) * len / (double) smax : 0;
+    }
+  };
+  if (nth <= 1) cell(0, 1);
+  else {
     std::vector<std::thread> th;
-    for (unsigned k = 0; k < nth; k++)
-      th.emplace_back([&, k] {
-        for (size_t i = k; i < ncell; i += nth) {
-          const double len = g[i + 1] - g[i];
-          cost[i] = len > 0 ? leaves(g[i], g[i + 1]) + c_level * levels(g[i]) * len / (double) smax : 0;
-        }
-      });
-    for (auto& t : th) t.join();
+    for (unsigned k = 0; k < nth; k++) th.emplace_back(cell, k, nth);
+    for (auto& h : th) h.join();
   }
-  std::vector<double> cum(g.size(), 0.0);
-  for (size_t i = 0; i < ncell; i++) cum[i + 1] = cum[i] + cost[i];
-  const double total = cum.back();
+  cum[0] = 0;
+  for (int i = 0; i < G; i++) cum[i + 1] = cum[i] + cost[i];
+  const double total = cum[G];
   const double target = std::max(total / (grid * 6.0), 1.0);
   // cumulative cost at n (linear inside a grid cell)
   auto C = [&](double n) {
-    size_t i = std::upper_bound(g.begin(), g.end(), n) - g.begin();
+    const int i = (int) (std::upper_bound(g, g + G + 1, n) - g);
     if (i == 0) return 0.0;
-    if (i >= g.size()) return total;
-    double f = (g[i] > g[i - 1]) ? (n - g[i - 1]) / (g[i] - g[i - 1]) : 0;
+    if (i > G) return total;
+    const double f = (g[i] > g[i - 1]) ? (n - g[i - 1]) / (g[i] - g[i - 1]) : 0;
     return cum[i - 1] + f * (cum[i] - cum[i - 1]);
   };
   // largest n with C(n) <= v (C is piecewise linear and non-decreasing)
   auto Cinv = [&](double v) {
     if (v >= total) return (double) L;
-    const size_t i = std::upper_bound(cum.begin(), cum.end(), v) - cum.begin();   // cum[i - 1] <= v < cum[i]
+    const int i = (int) (std::upper_bound(cum, cum + G + 1, v) - cum);   // cum[i - 1] <= v < cum[i]
     const double d = cum[i] - cum[i - 1];
     const double f = d > 0 ? (v - cum[i - 1]) / d : 0;
     return g[i - 1] + f * (g[i] - g[i - 1]);
   };
-  std::vector<int64_t> seg;
   int64_t a = 0;
-  seg.push_back(0);
+  if (!push(a)) return false;
   while (a < L) {
     const int64_t lo = a + 240, hi = std::min(a + smax, L);
-    if (hi <= lo) { a = std::min(a + smax, L); seg.push_back(a); continue; }
+    if (hi <= lo) {
+      a = std::min(a + smax, L);
+      if (!push(a)) return false;
+      continue;
+    }
     // the largest end (a multiple of 240, or hi) with cost <= target
     const double n = Cinv(C((double) a) + target);
     int64_t best = n >= (double) hi ? hi : (int64_t) (n / 240) * 240;
     best = std::max(lo, std::min(best, hi));
     a = std::min(best, L);
-    seg.push_back(a);
+    if (!push(a)) return false;
   }
+  return true;
+}
+
+static std::vector<int64_t> plan_segments(const SweepProblem& pb, const Tables& t, int64_t L, int64_t x_star,
+                                          int64_t pi_sqrt, int64_t bglob, int64_t smax, int grid)
+{
+  std::vector<double> dens((size_t) bglob + 1, 0.0);
+  for (int64_t b = 1; b <= bglob; b++) dens[b] = 0.56 / std::log(std::max((double) t.h_primes[(size_t) b], 3.0));
+  std::vector<int64_t> seg;
+  const unsigned nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  plan_segments_core(pb, t, L, x_star, pi_sqrt, bglob, smax, grid, dens.data(), nth,
+                     [&](int64_t v) { seg.push_back(v); return true; });
   return seg;
 }
 
@@ -1756,7 +1783,7 @@ struct CkptHeader {
   uint64_t plan_hash;
   int64_t next_first;      // first segment not swept yet
   int64_t waves;
-  uint64_t counters[4];
+  uint64_t counters[5];
 };
 
 static uint64_t plan_hash(const std::vector<int64_t>& seglo)
@@ -1976,7 +2003,7 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune_in, cud
   CkptHeader ck;
   memset(&ck, 0, sizeof(ck));
   memcpy(ck.magic, "PCGSWEEP", 8);
-  ck.version = 1;
+  ck.version = 2;
   ck.gourdon = pb.gourdon;
   ck.x_lo = (uint64_t) x;
   ck.x_hi = (uint64_t) (x >> 64);
@@ -2063,7 +2090,7 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune_in, cud
   }
   PCG_CUDA(cudaEventRecord(c.ev[1], s));
   std::vector<i128> acc((size_t) cols);
-  unsigned long long ctr[4];
+  unsigned long long ctr[5];
   PCG_CUDA(cudaMemcpyAsync(acc.data(), c.acc.p, (size_t) cols * 16, cudaMemcpyDeviceToHost, s));
   PCG_CUDA(cudaMemcpyAsync(ctr, d_counters, sizeof(ctr), cudaMemcpyDeviceToHost, s));
   if (pb.parts) {
@@ -2092,6 +2119,7 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune_in, cud
   st.two_prime_leaves = ctr[1];
   st.levels = ctr[2];
   st.factor_entries = ctr[3];
+  st.crossoff_multiples = ctr[4];
   st.segments = (uint64_t) nmine;
   st.kernel_launches = launches;
   if (use_ckpt) remove(tune.checkpoint.c_str());
@@ -2106,36 +2134,35 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune_in, cud
 
 
 // ================================================================ allocation-free D
-// Some callers cannot allocate device memory at the time they need D(x):
-// code that runs while a CUDA stream is being captured, serving loops that
-// must not touch the allocator on the request path, or hosts whose device
-// memory is owned by another framework's pool.  pcg_D_noalloc serves them:
-// it reads the tables a context built earlier (at set-up, when allocating was
-// allowed) and takes all of its working memory -- the per-(segment, level)
-// count and sign matrices, the segment and x/p tables, the counters and the
-// work queue -- from the file-scope array below.  Every GPU that loads this
-// library holds the array until the process exits.  All calls share it and
-// it keeps the previous call's contents, so everything that must start at
-// zero is cleared on the stream at the start of a call, and two calls whose
-// work overlaps on the GPU (different streams, or different host threads)
-// race on it; calls are serialised on the host by a mutex, but the caller
-// must not overlap them on the device.
+// Some callers cannot allocate device memory at the time they need D(x): a
+// serving loop that must not touch the allocator on its request path, or a
+// host whose device memory is owned by another framework's pool, where a
+// cudaMalloc would fail or would take memory the pool accounts for.
+// pcg_D_noalloc serves them: it reads the tables a context built earlier (at
+// set-up, when allocating was allowed) and takes all of its device working
+// memory -- the per-(segment, level) count and sign matrices, the segment
+// and x/p tables, the counters and the work queue -- from the file-scope
+// array below, and its host working memory from static arrays.  Every GPU
+// that loads this library holds the device array until the process exits.
+// All calls share it and it keeps the previous call's contents, so
+// everything that must start at zero is cleared on the stream at the start
+// of a call.  Calls are serialised on the host by a mutex and each call
+// waits for its own work before it returns (also when it fails), but two
+// calls whose work overlaps on the GPU race on the array.
 #define PCG_NOALLOC_SCRATCH_BYTES (64ull << 20)
 #define PCG_NOALLOC_MAX_COLS 32768
 #define PCG_NOALLOC_MAX_SEGS (1 << 20)
 static __device__ __align__(256) unsigned char g_noalloc_scratch[PCG_NOALLOC_SCRATCH_BYTES];
 
-// Device address of the scratch array for the current device.  Host code
-// only holds a host-side stand-in for the symbol, so the address comes from
-// cudaGetSymbolAddress, once per device with that device current; the first
-// call on a device does this set-up, so it should come before any stream
-// capture.
-static unsigned char* noalloc_scratch()
+// Device address of the scratch array for device dev.  Host code only holds
+// a host-side stand-in for the symbol, so the address comes from
+// cudaGetSymbolAddress, once per device with that device current (the
+// caller makes dev current).  The first call on a device does this set-up,
+// so it should come before any stream capture.
+static unsigned char* noalloc_scratch(int dev)
 {
   static std::mutex mu;
   static unsigned char* addr[64] = {nullptr};
-  int dev = 0;
-  PCG_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) fail(PCG_EINVAL, "device index out of range");
   std::lock_guard<std::mutex> g(mu);
   if (!addr[dev]) {
@@ -2150,90 +2177,22 @@ static unsigned char* noalloc_scratch()
   return addr[dev];
 }
 
-// The segment planner of run_sweep with fixed-size arrays: same grid, same
-// cost model, segments written to out[0 .. return value].
-static int64_t plan_segments_fixed(const SweepProblem& pb, const Tables& t, int64_t L, int64_t x_star,
-                                   int64_t pi_sqrt, int64_t bglob, int64_t smax, int grid, int64_t* out,
-                                   int64_t max_out)
-{
-  const double x = (double) pb.x;
-  const double y = (double) pb.y, z = (double) pb.z;
-  const int G = 1200;
-  double g[G + 1], cum[G + 1];
-  g[0] = 0;
-  const double a0 = 240;
-  const double ratio = std::pow((double) L / a0, 1.0 / (G - 1));
-  for (int i = 0; i < G; i++) g[i + 1] = std::min((double) L, a0 * std::pow(ratio, i));
-  g[G] = (double) L;
-  auto dens = [&](int64_t b) { return 0.56 / std::log(std::max((double) t.h_primes[(size_t) b], 3.0)); };
-  auto leaves = [&](double lo, double hi) {
-    double sum = 0;
-    double l1 = std::max(lo, 1.0);
-    for (int64_t b = pb.k + 1; b <= bglob; b++) {
-      const double p = (double) t.h_primes[(size_t) b], xp = x / p;
-      double mlo, mhi;
-      if (b <= pi_sqrt) { mlo = std::max(z / p, xp / hi); mhi = std::min({xp / (p * p), z, xp / l1}); }
-      else { mlo = std::max(p, xp / hi); mhi = std::min({xp / (p * p), y, xp / l1}); }
-      if (mhi <= mlo) continue;
-      sum += (b <= pi_sqrt) ? (mhi - mlo) * dens(b) : (mhi - mlo) / std::log(std::max(mhi, 3.0));
-    }
-    return sum;
-  };
-  auto levels = [&](double a) {
-    double lim = std::min((double) x_star, std::sqrt(x / std::max(a, 1.0)));
-    return (double) host_pi(t, (uint64_t) std::min(lim, (double) t.prime_limit));
-  };
-  const double c_level = 30.0;
-  cum[0] = 0;
-  for (int i = 0; i < G; i++) {
-    double len = g[i + 1] - g[i];
-    double c = len > 0 ? leaves(g[i], g[i + 1]) + c_level * levels(g[i]) * len / (double) smax : 0;
-    cum[i + 1] = cum[i] + c;
-  }
-  const double total = cum[G];
-  const double target = std::max(total / (grid * 6.0), 1.0);
-  auto C = [&](double n) {
-    int i = (int) (std::upper_bound(g, g + G + 1, n) - g);
-    if (i == 0) return 0.0;
-    if (i > G) return total;
-    double f = (g[i] > g[i - 1]) ? (n - g[i - 1]) / (g[i] - g[i - 1]) : 0;
-    return cum[i - 1] + f * (cum[i] - cum[i - 1]);
-  };
-  int64_t n = 0;
-  int64_t a = 0;
-  out[n++] = 0;
-  while (a < L) {
-    if (n >= max_out) return -1;
-    double ca = C((double) a);
-    int64_t lo = a + 240, hi = std::min(a + smax, L);
-    if (hi <= lo) { a = std::min(a + smax, L); out[n++] = a; continue; }
-    int64_t best = lo;
-    if (C((double) hi) - ca <= target) best = hi;
-    else {
-      int64_t l = lo / 240, h = hi / 240;
-      while (l < h) {
-        int64_t m = (l + h + 1) / 2;
-        if (C((double) (m * 240)) - ca <= target) l = m; else h = m - 1;
-      }
-      best = std::max(lo, l * 240);
-    }
-    a = std::min(best, L);
-    out[n++] = a;
-  }
-  return n - 1;
-}
-
 SweepResult run_sweep_noalloc(Ctx& c, const SweepProblem& pb, cudaStream_t s)
 {
   static std::mutex call_mu;
   static uint64_t h_xp[3 * PCG_NOALLOC_MAX_COLS];
+  static double h_dens[PCG_NOALLOC_MAX_COLS];
   static int64_t h_seg[PCG_NOALLOC_MAX_SEGS + 1];
+  static int64_t h_nseg = -1;
+  static int64_t h_plan_key[8];
   static i128 h_acc[PCG_NOALLOC_MAX_COLS];
   std::lock_guard<std::mutex> guard(call_mu);
   SweepResult res;
   pcg_stats& st = res.stats;
   double t_start = now_ms();
-  unsigned char* scratch = noalloc_scratch();
+  // the context's device, whichever device the calling thread has current
+  PCG_CUDA(cudaSetDevice(c.device));
+  unsigned char* scratch = noalloc_scratch(c.device);
   const u128 x = pb.x;
   const Tables& T = c.tab;
   // the tables are inputs: they must already be resident (no building here)
@@ -2274,9 +2233,25 @@ SweepResult run_sweep_noalloc(Ctx& c, const SweepProblem& pb, cudaStream_t s)
   else occupancy_sweep<uint32_t, 256>(&occ, smem);
   const int ctas = std::max(occ, 1);
   const int grid = c.num_sms * ctas;
-  const int64_t nseg = plan_segments_fixed(pb, T, L, x_star, pi_sqrt, bglob, (int64_t) words * 240, grid, h_seg,
-                                           PCG_NOALLOC_MAX_SEGS);
-  if (nseg < 0) fail(PCG_ERANGE, "pcg_D_noalloc: too many segments for the fixed segment table");
+  // the segment plan of run_sweep's planner, costed on this thread and kept
+  // for the next call with the same problem and launch shape
+  const int64_t key[8] = {(int64_t) (uint64_t) x, (int64_t) (uint64_t) (x >> 64), pb.y, pb.z, pb.k, words, grid,
+                          (int64_t) T.prime_limit};
+  if (h_nseg < 0 || memcmp(key, h_plan_key, sizeof(key)) != 0) {
+    for (int64_t b = 1; b <= bglob; b++) h_dens[b] = 0.56 / std::log(std::max((double) T.h_primes[(size_t) b], 3.0));
+    int64_t n = 0;
+    h_nseg = -1;
+    const bool ok = plan_segments_core(pb, T, L, x_star, pi_sqrt, bglob, (int64_t) words * 240, grid, h_dens, 1,
+                                       [&](int64_t v) {
+                                         if (n > PCG_NOALLOC_MAX_SEGS) return false;
+                                         h_seg[n++] = v;
+                                         return true;
+                                       });
+    if (!ok) fail(PCG_ERANGE, "pcg_D_noalloc: too many segments for the fixed segment table");
+    h_nseg = n - 1;
+    memcpy(h_plan_key, key, sizeof(key));
+  }
+  const int64_t nseg = h_nseg;
 
   // carve the scratch: counters and queue, x/p table, segment table, run,
   // acc, segsum, then the count and sign matrices with as many rows as fit
@@ -2307,13 +2282,6 @@ SweepResult run_sweep_noalloc(Ctx& c, const SweepProblem& pb, cudaStream_t s)
   int32_t* d_smu = (int32_t*) (scratch + off);
   off = align(off + (size_t) wave_len * cols * 4);
   if (off > PCG_NOALLOC_SCRATCH_BYTES) fail(PCG_EINTERNAL, "no-alloc scratch carve overflow");
-
-  // everything that must start at zero
-  PCG_CUDA(cudaMemsetAsync(d_counters, 0, 4096, s));
-  PCG_CUDA(cudaMemsetAsync(d_run, 0, (size_t) cols * 8, s));
-  PCG_CUDA(cudaMemsetAsync(d_acc, 0, (size_t) cols * 16, s));
-  PCG_CUDA(cudaMemcpyAsync(d_xp, h_xp, (size_t) cols * 24, cudaMemcpyHostToDevice, s));
-  PCG_CUDA(cudaMemcpyAsync(d_seg, h_seg, (size_t) (nseg + 1) * 8, cudaMemcpyHostToDevice, s));
 
   SweepArgs a;
   memset(&a, 0, sizeof(a));
@@ -2347,28 +2315,42 @@ SweepResult run_sweep_noalloc(Ctx& c, const SweepProblem& pb, cudaStream_t s)
   a.counters = d_counters;
   uint64_t launches = 0;
   int waves = 0;
-  for (int64_t first = 0; first < nseg; first += wave_len) {
-    int wl = (int) std::min<int64_t>(wave_len, nseg - first);
-    a.wave_first = first;
-    a.wave_len = wl;
-    a.queue = d_queue + (waves % 16);
-    PCG_CUDA(cudaMemsetAsync(d_cnt, 0, (size_t) wl * cols * 4, s));
-    PCG_CUDA(cudaMemsetAsync(d_smu, 0, (size_t) wl * cols * 4, s));
-    if (waves % 16 == 0 && waves > 0) PCG_CUDA(cudaMemsetAsync(d_queue, 0, 64, s));
-    int g = (int) std::min<int64_t>(grid, wl);
-    if (fbytes == 2) launch_sweep<uint16_t, 256>(a, g, smem, s);
-    else launch_sweep<uint32_t, 256>(a, g, smem, s);
-    PCG_CUDA(cudaGetLastError());
-    k_combine<<<(cols + 31) / 32, 32 * COMBINE_WARPS, 0, s>>>(d_cnt, d_smu, wl, cols, d_run, d_acc, nullptr);
-    k_segsum<<<1, 1024, 0, s>>>(d_segsum, wl, d_acc);
-    PCG_CUDA(cudaGetLastError());
-    launches += 3;
-    waves++;
+  unsigned long long ctr[5];
+  try {
+    // everything that must start at zero, then the call's inputs
+    PCG_CUDA(cudaMemsetAsync(d_counters, 0, 4096, s));
+    PCG_CUDA(cudaMemsetAsync(d_run, 0, (size_t) cols * 8, s));
+    PCG_CUDA(cudaMemsetAsync(d_acc, 0, (size_t) cols * 16, s));
+    PCG_CUDA(cudaMemcpyAsync(d_xp, h_xp, (size_t) cols * 24, cudaMemcpyHostToDevice, s));
+    PCG_CUDA(cudaMemcpyAsync(d_seg, h_seg, (size_t) (nseg + 1) * 8, cudaMemcpyHostToDevice, s));
+    for (int64_t first = 0; first < nseg; first += wave_len) {
+      int wl = (int) std::min<int64_t>(wave_len, nseg - first);
+      a.wave_first = first;
+      a.wave_len = wl;
+      a.queue = d_queue + (waves % 16);
+      PCG_CUDA(cudaMemsetAsync(d_cnt, 0, (size_t) wl * cols * 4, s));
+      PCG_CUDA(cudaMemsetAsync(d_smu, 0, (size_t) wl * cols * 4, s));
+      if (waves % 16 == 0 && waves > 0) PCG_CUDA(cudaMemsetAsync(d_queue, 0, 64, s));
+      int g = (int) std::min<int64_t>(grid, wl);
+      if (fbytes == 2) launch_sweep<uint16_t, 256>(a, g, smem, s);
+      else launch_sweep<uint32_t, 256>(a, g, smem, s);
+      PCG_CUDA(cudaGetLastError());
+      k_combine<<<(cols + 31) / 32, 32 * COMBINE_WARPS, 0, s>>>(d_cnt, d_smu, wl, cols, d_run, d_acc, nullptr);
+      k_segsum<<<1, 1024, 0, s>>>(d_segsum, wl, d_acc);
+      PCG_CUDA(cudaGetLastError());
+      launches += 3;
+      waves++;
+    }
+    PCG_CUDA(cudaMemcpyAsync(h_acc, d_acc, (size_t) cols * 16, cudaMemcpyDeviceToHost, s));
+    PCG_CUDA(cudaMemcpyAsync(ctr, d_counters, sizeof(ctr), cudaMemcpyDeviceToHost, s));
+    PCG_CUDA(cudaStreamSynchronize(s));
+  } catch (...) {
+    // work already queued may still use the scratch: wait for it before the
+    // mutex lets the next call clear and refill the array
+    cudaStreamSynchronize(s);
+    cudaGetLastError();
+    throw;
   }
-  unsigned long long ctr[4];
-  PCG_CUDA(cudaMemcpyAsync(h_acc, d_acc, (size_t) cols * 16, cudaMemcpyDeviceToHost, s));
-  PCG_CUDA(cudaMemcpyAsync(ctr, d_counters, sizeof(ctr), cudaMemcpyDeviceToHost, s));
-  PCG_CUDA(cudaStreamSynchronize(s));
   i128 sum = 0;
   for (int b = 0; b < cols; b++) sum += h_acc[b];
   res.sum = sum;
@@ -2376,6 +2358,7 @@ SweepResult run_sweep_noalloc(Ctx& c, const SweepProblem& pb, cudaStream_t s)
   st.two_prime_leaves = ctr[1];
   st.levels = ctr[2];
   st.factor_entries = ctr[3];
+  st.crossoff_multiples = ctr[4];
   st.segments = (uint64_t) nseg;
   st.kernel_launches = launches;
   st.sweep_launches = (uint64_t) waves;

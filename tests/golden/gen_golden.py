@@ -11,17 +11,19 @@ the reference):
   - test/api/api.cpp:112-116            (phi(1e12, 78498))
   - test/gourdon/pi_gourdon.cpp:94-106  (pi(1e11), pi(1e12))
 * the reference binary compiled from its sources by oracle/ref.mk
-  (oracle/_ref/primecount), run for D, S2_hard, pi and phi at further
+  (oracle/_ref/<cpu arch>/primecount), run for D, S2_hard, pi and phi at further
   inputs.  Parameters (y, z, k / c) are read from its --status output.
 
-Usage:  python tests/golden/gen_golden.py [--ref /root/reference] [--big]
---big adds the multi-minute inputs (D and S2_hard at 1e19..1e21).
+Usage:  python tests/golden/gen_golden.py [--ref <primecount source tree>] [--big]
+--ref defaults to the environment variable PCG_REFERENCE.  --big adds the
+multi-minute inputs (D at 1e19..1e22, S2_hard at 1e19..1e20).
 Existing entries in the fixture are kept, so expensive values are computed
 once.
 """
 import argparse
 import json
 import os
+import platform
 import random
 import re
 import subprocess
@@ -30,7 +32,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 OUT = os.path.join(HERE, "hard_leaves.json")
-BIN = os.path.join(ROOT, "oracle", "_ref", "primecount")
+BIN = os.path.join(ROOT, "oracle", "_ref", platform.machine(), "primecount")
 
 
 def tuples(path):
@@ -70,10 +72,12 @@ def run_status(x, opt):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("PCG_REFERENCE"))
     ap.add_argument("--big", action="store_true")
     a = ap.parse_args()
     ref = a.ref
+    if not ref:
+        sys.exit("pass --ref <primecount source tree> or set PCG_REFERENCE")
 
     data = {}
     if os.path.exists(OUT):
@@ -100,7 +104,7 @@ def main():
     sx = data.setdefault("S2_hard_default", {})
     exps = [15, 16, 17, 18]
     if a.big:
-        exps += [19, 20, 21]
+        exps += [19, 20, 21, 22]
     for e in exps:
         x = 10 ** e
         if str(x) not in dx:

@@ -85,9 +85,10 @@ def test_pi_other_alpha(pcg, golden):
             assert pcg.pi(x, alpha_y=ay, alpha_z=az) == want, (x, ay, az)
 
 
-def test_pi_1e20_and_1e21(pcg, golden):
-    # the 128-bit path end to end: x = 1e21 > 2^64 (README of the reference)
-    for n in (20, 21):
+def test_pi_int128_configs(pcg, golden):
+    # the 128-bit path end to end: x = 1e20, 1e21, 1e22 > 2^64, against the
+    # reference's published pi(10^n) (README.md:253-277)
+    for n in (20, 21, 22):
         x = 10 ** n
         assert pcg.pi(x) == golden["pi_pow10"][str(x)], n
 
