@@ -204,59 +204,77 @@ def port_sample(p, threads, target_s=12.0):
                       % (nchunks, nchunks, frac, leaves, secs, threads)}
 
 
-def batch_workload(n, seed=20261203):
-    """Seeded batch: n pi(x), x = 10^U(10,18); n phi(x, a), x = 10^U(8,16),
-    a = U{1, pi(sqrt x)} (std::mt19937_64 is not needed for determinism:
-    Python's seeded generator fixes the inputs and they are printed in the
-    config)."""
+BATCH_FIXTURE = os.path.join(ROOT, "tests", "golden", "batch_4096.json")
+
+
+def batch_workload(n, pcg):
+    """The seeded batch (4096 pi(x), x = floor(10^U(10,18)); 4096 phi(x, a),
+    x = floor(10^U(8,16)), a = 1 + floor(u pi(floor(sqrt x))); seed 20261203)
+    with the reference's answers, from the committed fixture
+    (tests/golden/gen_batch.py); without it, the same generator and no
+    reference answers."""
+    if os.path.exists(BATCH_FIXTURE):
+        d = json.load(open(BATCH_FIXTURE))
+        if d.get("n", 0) >= n:
+            xs = [int(v) for v in d["pi_x"][:n]]
+            px = [int(v) for v in d["phi_x"][:n]]
+            pa = d["phi_a"][:n]
+            if all(a is not None for a in pa):
+                return (xs, [None if v is None else int(v) for v in d["pi"][:n]], px, [int(a) for a in pa],
+                        [None if v is None else int(v) for v in d["phi"][:n]], "tests/golden/batch_4096.json")
     import math
-    import random
-    rng = random.Random(seed)
-    xs = [int(10 ** rng.uniform(10, 18)) for _ in range(n)]
-    px = [int(10 ** rng.uniform(8, 16)) for _ in range(n)]
-    us = [rng.random() for _ in range(n)]
-    return xs, px, us
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import gen_batch
+    xs, px, us = gen_batch.inputs(n)
+    pis = pcg.pi_batch([math.isqrt(x) for x in px])
+    pa = [1 + int(u * max(1, p)) for u, p in zip(us, pis)]
+    return xs, [None] * n, px, pa, [None] * n, "generated (no fixture)"
 
 
 def run_batch(args, pcg):
-    import math
     import torch
     n = args.batch
-    xs, px, us = batch_workload(n)
-    sq = [math.isqrt(x) for x in px]
-    pis = pcg.pi_batch(sq)
-    pa = [1 + int(u * max(1, p)) for u, p in zip(us, pis)]
+    xs, want_pi, px, pa, want_phi, src = batch_workload(n, pcg)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     r_pi = pcg.pi_batch(xs)
     t1 = time.perf_counter()
     r_phi = pcg.phi_batch(px, pa)
     t2 = time.perf_counter()
+    checked = [(g, w) for g, w in zip(r_pi + r_phi, want_pi + want_phi) if w is not None]
+    bad = sum(1 for g, w in checked if g != w)
+    if bad:
+        raise SystemExit("batch: %d answers differ from the reference fixture" % bad)
     m = min(args.plain_sample, n)
-    # plain: one query per call, tables built inside (fresh context)
+    # plain: one query per call, tables built inside (fresh context), on an
+    # evenly spread sample of the same queries
+    idx = [(i * n) // m for i in range(m)]
     tp = []
-    for i in range(m):
-        c = pcg.Context(0)
-        a0 = time.perf_counter()
-        v = pcg.pi(xs[i], ctx=c)
-        tp.append(("pi", time.perf_counter() - a0))
-        assert v == r_pi[i]
-        c.close()
-        c = pcg.Context(0)
-        a0 = time.perf_counter()
-        v = pcg.phi(px[i], pa[i], ctx=c)
-        tp.append(("phi", time.perf_counter() - a0))
-        assert v == r_phi[i]
-        c.close()
-    plain_pi = [t for k, t in tp if k == "pi"]
-    plain_phi = [t for k, t in tp if k == "phi"]
-    return {"queries": {"pi": n, "phi": n}, "seed": 20261203,
+    for i in idx:
+        for kind in ("pi", "phi"):
+            c = pcg.Context(0)
+            a0 = time.perf_counter()
+            v = pcg.pi(xs[i], ctx=c) if kind == "pi" else pcg.phi(px[i], pa[i], ctx=c)
+            tp.append((kind, time.perf_counter() - a0))
+            c.close()
+            if v != (r_pi[i] if kind == "pi" else r_phi[i]):
+                raise SystemExit("batch: the plain answer differs from the batched one (%s, %d)" % (kind, i))
+    plain_pi = sorted(t for k, t in tp if k == "pi")
+    plain_phi = sorted(t for k, t in tp if k == "phi")
+
+    def p99(v):
+        return v[min(len(v) - 1, int(round(0.99 * (len(v) - 1))))] if v else None
+    return {"queries": {"pi": n, "phi": n}, "seed": 20261203, "inputs": src,
             "engine": {"pi_qps": n / (t1 - t0), "phi_qps": n / (t2 - t1), "all_qps": 2 * n / (t2 - t0),
-                       "seconds": t2 - t0},
+                       "seconds": t2 - t0, "pi_seconds": t1 - t0, "phi_seconds": t2 - t1,
+                       "latency_note": "one call per kind: every query of a call completes when the call returns "
+                                       "(p99 latency = the call's wall time)"},
             "plain_sample": {"queries_per_kind": m, "pi_qps": len(plain_pi) / max(sum(plain_pi), 1e-9),
                              "phi_qps": len(plain_phi) / max(sum(plain_phi), 1e-9),
-                             "note": "first queries of the same seeded batch, one per call, fresh context"},
-            "checks": "plain answers equal the batched ones on the sample"}
+                             "pi_p99_s": p99(plain_pi), "phi_p99_s": p99(plain_phi),
+                             "note": "evenly spread queries of the same batch, one per call, fresh context"},
+            "checks": {"reference_answers_checked": len(checked), "mismatches": bad,
+                       "plain_equal_batched": True}}
 
 
 def run_reference(args, rank):
@@ -327,12 +345,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--x", default="1e20", help="smaller x for profiling runs (the headline is 1e20)")
     ap.add_argument("--pi-steps", type=int, default=1, help="pi(x) end-to-end repetitions")
-    ap.add_argument("--batch", type=int, default=256,
+    ap.add_argument("--batch", type=int, default=4096,
                     help="queries per kind of the batched workload (4096 = the full config; 0 = skip)")
-    ap.add_argument("--plain-sample", type=int, default=24, help="queries per kind timed in the plain form")
-    ap.add_argument("--serve-seconds", type=float, default=0, help="serving stream length (0 = skip)")
+    ap.add_argument("--plain-sample", type=int, default=32, help="queries per kind timed in the plain form")
+    ap.add_argument("--serve-seconds", type=float, default=60, help="serving stream length (0 = skip)")
+    ap.add_argument("--serve-drain", type=float, default=10, help="seconds to finish admitted requests")
     ap.add_argument("--serve-budget", type=float, default=2.0,
-                    help="serving admission budget in estimated GPU-seconds (0 = admit everything)")
+                    help="serving latency budget in estimated GPU-seconds (0 = admit everything)")
     args = ap.parse_args()
     global X
     X = int(float(args.x)) if "e" in args.x else int(args.x)
@@ -460,13 +479,22 @@ def main():
         from primecount_gb300 import serve as sv
         stream = sv.make_stream(20261203, 2000, args.serve_seconds)
         budget = args.serve_budget if args.serve_budget > 0 else None
-        r = sv.run_served(stream, workers=8, max_x=10 ** 20, drain_s=30, latency_budget=budget)
+        r = sv.run_served(stream, workers=8, max_x=10 ** 20, drain_s=args.serve_drain, latency_budget=budget)
         r.pop("results")
-        plain = sv.run_plain(stream, drain_s=30, latency_budget=budget)
+        served_answers = r.pop("requests")
+        plain = sv.run_plain(stream, drain_s=args.serve_drain, latency_budget=budget,
+                             cost=sv.cost_from(r["cost_model"]))
+        # every served answer against the same query computed alone (an evenly spread sample)
+        step = max(1, len(served_answers) // 64)
+        sample = served_answers[::step]
+        alone_ok = all((pcg.pi(x) if k == "pi" else pcg.phi(x, a)) == v for k, x, a, v in sample)
+        if not alone_ok:
+            raise SystemExit("serve: an answer in the mix differs from the same query alone")
         serve = {"served": r, "plain": plain,
+                 "checks": {"served_equal_alone_sample": len(sample)},
                  "config": {"rate": 2000, "seconds": args.serve_seconds, "seed": 20261203,
                             "pi_x": "10^U(8,20)", "phi_x": "10^U(8,16)", "requests": len(stream),
-                            "latency_budget_s": budget, "workers": 8}}
+                            "latency_budget_s": budget, "workers": 8, "drain_s": args.serve_drain}}
 
     if rank != 0:
         return

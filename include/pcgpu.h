@@ -144,6 +144,22 @@ enum {
 pcg_status pcg_ctx_read_table(const pcg_ctx* ctx, int table, uint64_t first, uint64_t count, void* out,
                               uint64_t* entries, int* entry_bytes, int64_t* limit);
 
+/* ---- serving support (no counterpart in the reference) ---- */
+
+enum { PCG_QUERY_PI = 0, PCG_QUERY_PHI = 1 };
+/* Device working memory (bytes) that one pi(x) (kind PCG_QUERY_PI) or
+ * phi(x, a) (PCG_QUERY_PHI) call on ctx needs beyond ctx's resident tables:
+ * the sweep's count and sign rows and tables, the prime sieve's buffers, the
+ * formulas' temporaries and any table the call would still have to build.
+ * An estimate from the call's sizes, at or above what the call allocates;
+ * for admission control by a serving loop.  ctx NULL: the default context. */
+pcg_status pcg_query_device_bytes(const pcg_ctx* ctx, int kind, pcg_i128 x, int64_t a, uint64_t* bytes);
+/* Frees the per-call working memory ctx keeps between calls (the resident
+ * tables stay); *freed (may be NULL) receives the bytes released. */
+pcg_status pcg_ctx_trim(pcg_ctx* ctx, uint64_t* freed);
+/* Free and total memory of the current CUDA device. */
+pcg_status pcg_device_memory(uint64_t* free_bytes, uint64_t* total_bytes);
+
 /* ---- the hard-leaf formulas ---- */
 
 /* D(x, y, z, k): Gourdon's hard special leaves. */

@@ -125,6 +125,12 @@ def load(path=None):
     L.pcg_ctx_read_table.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64,
                                      ctypes.c_void_p, c_p(ctypes.c_uint64), c_p(ctypes.c_int), c_p(c_i64)]
     L.pcg_ctx_read_table.restype = ctypes.c_int
+    L.pcg_query_device_bytes.argtypes = [ctypes.c_void_p, ctypes.c_int, I128, c_i64, c_p(ctypes.c_uint64)]
+    L.pcg_query_device_bytes.restype = ctypes.c_int
+    L.pcg_ctx_trim.argtypes = [ctypes.c_void_p, c_p(ctypes.c_uint64)]
+    L.pcg_ctx_trim.restype = ctypes.c_int
+    L.pcg_device_memory.argtypes = [c_p(ctypes.c_uint64), c_p(ctypes.c_uint64)]
+    L.pcg_device_memory.restype = ctypes.c_int
     L.pcg_autotune.argtypes = [I128, c_p(Opts), c_p(Tuning)]
     L.pcg_autotune.restype = ctypes.c_int
     for name in ("pcg_D", "pcg_S2_hard", "pcg_D_default", "pcg_S2_hard_default", "pcg_gourdon_params",
@@ -172,6 +178,13 @@ class Context:
         s = Stats()
         _check(load().pcg_last_stats(self._h, ctypes.byref(s)), self)
         return s.as_dict()
+
+    def trim(self):
+        """Free the per-call working memory kept between calls (pcg_ctx_trim);
+        the resident tables stay.  Returns the bytes released."""
+        f = ctypes.c_uint64()
+        _check(load().pcg_ctx_trim(self._h, ctypes.byref(f)), self)
+        return f.value
 
     TABLES = {"primes": 0, "pi": 1, "factor_d": 2, "factor_dr": 3}
 
@@ -310,6 +323,22 @@ def phi_batch(xs, as_, ctx=None, stream=None):
     o = _opts(ctx, stream)
     _check(load().pcg_phi_batch(ax, aa, n, out, ctypes.byref(o)), ctx)
     return list(out)
+
+
+def query_device_bytes(kind, x, a=0, ctx=None):
+    """Device working memory of one pi(x) ("pi") or phi(x, a) ("phi") call
+    beyond the resident tables of ctx (pcg_query_device_bytes)."""
+    b = ctypes.c_uint64()
+    _check(load().pcg_query_device_bytes(ctx._h if ctx is not None else None, 0 if kind == "pi" else 1,
+                                         to_i128(x), int(a or 0), ctypes.byref(b)), ctx)
+    return b.value
+
+
+def device_memory():
+    """(free, total) bytes of the current CUDA device (pcg_device_memory)."""
+    f, t = ctypes.c_uint64(), ctypes.c_uint64()
+    _check(load().pcg_device_memory(ctypes.byref(f), ctypes.byref(t)))
+    return f.value, t.value
 
 
 # ---------------------------------------------------------------- shards

@@ -638,6 +638,111 @@ pcg_status pcg_ctx_read_table(const pcg_ctx* ctx, int table, uint64_t first, uin
   });
 }
 
+// ---- serving support: device memory of a query, trimming, free memory
+static int64_t pi_estimate(const Ctx& c, int64_t v)
+{
+  if (v < 2) return 0;
+  if (v <= c.tab.prime_limit) return host_pi(c.tab, (uint64_t) v);
+  const double d = (double) v;
+  return (int64_t) (1.26 * d / std::log(d)) + 1;   // above pi(v) for v >= 17
+}
+
+static uint64_t table_bytes_beyond(const Ctx& c, int64_t y, int64_t z, int64_t sqrtx)
+{
+  uint64_t b = 0;
+  if (y > c.tab.prime_limit) b += (uint64_t) (y / 240 + 1) * (16 + 20) + (uint64_t) pi_estimate(c, y) * 12;
+  if (z > c.tab.fd_z) b += (uint64_t) (wheel2310().to_index((uint64_t) z) + 1) * (2 + 8);
+  if (sqrtx + 240 > c.tab.pibig_limit) b += (uint64_t) (sqrtx / 240 + 2) * (16 + 20);
+  return b;
+}
+
+// B's prime sieve over [lo, hi): per-segment sums and the sieving primes
+static uint64_t psieve_bytes(int64_t lo, int64_t hi)
+{
+  if (hi <= lo) return 0;
+  const int64_t seg = 12288ll * 240;
+  return (uint64_t) ((hi - lo) / seg + 2) * 24 + (uint64_t) (isqrt((u128) hi) / 8 + 64) * 12;
+}
+
+static uint64_t pi_query_bytes(const Ctx& c, u128 x)
+{
+  if (x <= (u128) 10000000000ull) return psieve_bytes(0, (int64_t) x + 1) + 4096;
+  const GourdonParams g = gourdon_params(x);
+  const int64_t sqrtx = isqrt(x);
+  const int64_t cols = pi_estimate(c, g.x_star) + 1;
+  uint64_t b = sweep_device_bytes(c.num_sms, (int64_t) (x / (u128) g.z), cols, 8192);
+  b += psieve_bytes(sqrtx, (int64_t) (x / (u128) g.y) + 1);
+  b += (uint64_t) pi_estimate(c, iroot(x, 3)) * 4 * 64;      // A + C outer terms
+  b += table_bytes_beyond(c, g.y, g.z, sqrtx);
+  return b + 65536;
+}
+
+}  // extern "C"
+
+namespace pcg {
+// device bytes of one phi(x, a) query beyond the context's resident tables
+static uint64_t phi_query_bytes(const Ctx& c, int64_t x, int64_t a)
+{
+  if (x < 1 || a <= 8 || a > x / 2) return 4096;
+  const int64_t sq = isqrt((u128) x);
+  const int64_t pis = pi_estimate(c, sq);
+  if (a > pis) return pi_query_bytes(c, (u128) x);
+  const double la = std::log((double) std::max<int64_t>(a, 3));
+  const int64_t pa = (int64_t) ((double) a * (la + std::log(std::max(la, 1.0))));   // above p_a for a >= 6
+  if ((u128) pa * pa * pa * pa > (u128) x)                    // P2 + P3
+    return pi_query_bytes(c, (u128) x) + psieve_bytes(sq, x / std::max<int64_t>(pa / 2, 1) + 1) +
+           (uint64_t) pi_estimate(c, iroot((u128) x, 3)) * 64;
+  const int64_t y = std::max<int64_t>(pa, std::min<int64_t>(sq - 1, 8 * iroot((u128) x, 3)));
+  uint64_t b = sweep_device_bytes(c.num_sms, x / y, a + 1, 8192);
+  b += (uint64_t) (wheel2310().to_index((uint64_t) y) + 1) * (2 + 8) + (uint64_t) (y / 240 + 1) * 36;
+  b += (uint64_t) c.num_sms * 8 * 16;                         // the ordinary leaves' partial sums
+  return b + 65536;
+}
+}  // namespace pcg
+
+extern "C" {
+
+pcg_status pcg_query_device_bytes(const pcg_ctx* ctx, int kind, pcg_i128 x, int64_t a, uint64_t* bytes)
+{
+  if (!bytes) return PCG_EINVAL;
+  return guard(nullptr, [&] {
+    const Ctx& c = ctx ? *(const Ctx*) ctx : default_ctx();
+    if (x.hi < 0) { *bytes = 0; return; }
+    if (kind == PCG_QUERY_PI) *bytes = pi_query_bytes(c, make_u128(x));
+    else if (kind == PCG_QUERY_PHI) {
+      if (x.hi != 0 || x.lo > (uint64_t) INT64_MAX) fail(PCG_ERANGE, "phi(x, a): x must fit int64");
+      *bytes = phi_query_bytes(c, (int64_t) x.lo, a);
+    } else fail(PCG_EINVAL, "kind must be PCG_QUERY_PI or PCG_QUERY_PHI");
+  });
+}
+
+pcg_status pcg_ctx_trim(pcg_ctx* ctx, uint64_t* freed)
+{
+  if (!ctx) return PCG_EINVAL;
+  return guard(ctx, [&] {
+    std::lock_guard<std::recursive_mutex> lk(ctx->call_mu);
+    PCG_CUDA(cudaSetDevice(ctx->device));
+    PCG_CUDA(cudaStreamSynchronize(ctx->stream));
+    const uint64_t f = ctx_trim(*ctx);
+    if (freed) *freed = f;
+  });
+}
+
+pcg_status pcg_device_memory(uint64_t* free_bytes, uint64_t* total_bytes)
+{
+  return guard(nullptr, [&] {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+      cudaGetLastError();
+      fail(PCG_ENODEV, "no CUDA device");
+    }
+    size_t f = 0, t = 0;
+    PCG_CUDA(cudaMemGetInfo(&f, &t));
+    if (free_bytes) *free_bytes = f;
+    if (total_bytes) *total_bytes = t;
+  });
+}
+
 pcg_status pcg_D_default(pcg_i128 xi, const pcg_opts* opts, pcg_i128* out, int64_t* y, int64_t* z, int64_t* k)
 {
   int64_t yy = 1, zz = 1, kk = 0, xs = 0;

@@ -875,7 +875,9 @@ static cudaStream_t aux_stream(Ctx& c)
   return c.aux;
 }
 
-static PiParts pi_gourdon(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s)
+// with_d = false leaves D out (R.d = 0, R.pi without it): the batch form
+// computes the D of all its queries in one batched sweep
+static PiParts pi_gourdon(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s, bool with_d = true)
 {
   PiParts R;
   GourdonParams g = gourdon_params(x, tune.alpha_y, tune.alpha_z);
@@ -1055,7 +1057,9 @@ static PiParts pi_gourdon(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s)
     }
   };
   uint64_t launches2 = 0;
-  if (pi_overlap()) {
+  if (!with_d) {
+    other_terms(s, &launches2);
+  } else if (pi_overlap()) {
     cudaStream_t s2 = aux_stream(c);
     PCG_CUDA(cudaEventRecord(c.ev[2], s));          // the tables are built on s
     PCG_CUDA(cudaStreamWaitEvent(s2, c.ev[2], 0));
@@ -1113,6 +1117,18 @@ i128 pi_any(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s, pcg_stats* st)
   z.total_ms = fnow_ms() - t0;
   if (st) *st = z;
   return r;
+}
+
+// pi(x) without Gourdon's D term (x > 1e10), or pi(x) itself (x <= 1e10,
+// counted by the sieve): *needs_d tells whether D must still be added
+i128 pi_without_d(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s, bool* needs_d)
+{
+  if (x <= (u128) PI_SIEVE_LIMIT) {
+    *needs_d = false;
+    return pi_any(c, x, tune, s, nullptr);
+  }
+  *needs_d = true;
+  return pi_gourdon(c, x, tune, s, false).pi;
 }
 
 // per-term values of Gourdon's formula (for parity tests against the

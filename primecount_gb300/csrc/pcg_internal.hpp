@@ -124,7 +124,7 @@ enum TmpSlot {
   T_AC_QLO, T_AC_QCNT, T_AC_QOFF, T_AC_OUTS,                  // A + C outers
   T_PR_PIECES, T_PR_FIRST, T_PR_SPLIT, T_PR_PART, T_PR_SUMS,  // pair sums
   T_PHI0_PART, T_PHI_ONE, T_PHI_OUTS,                         // Phi0, phi(x, a)
-  T_SW_SEG, T_SW_XP,                                          // sweep segment and x/p tables
+  T_SW_SEG, T_SW_XP, T_SW_Q, T_SW_ROW, T_SW_JOB,              // sweep: segments, x/p, problems, rows, jobs
   T_COUNT
 };
 // PiTable {count, bits} over [0, limit] without the primes array
@@ -168,6 +168,14 @@ struct SweepResult {
 };
 
 SweepResult run_sweep(Ctx& c, const SweepProblem& p, const Tuning& t, cudaStream_t s);
+// D of many problems (gourdon = 1, y >= z each) in one sweep whose waves run
+// as one CUDA graph; sums[i] = D of pbs[i]
+void run_sweep_batch(Ctx& c, const std::vector<SweepProblem>& pbs, const Tuning& t, cudaStream_t s,
+                     std::vector<i128>& sums, pcg_stats* st);
+// device working memory of one sweep over [0, L) with cols columns
+uint64_t sweep_device_bytes(int num_sms, int64_t L, int64_t cols, int words);
+// frees a context's per-call working memory (the tables stay); bytes freed
+uint64_t ctx_trim(Ctx& c);
 // D with working memory from a static device array; tables must be resident
 SweepResult run_sweep_noalloc(Ctx& c, const SweepProblem& p, cudaStream_t s);
 
@@ -185,7 +193,7 @@ struct Ctx {
   // per-call temporaries, one slot per use site, kept and grown across calls
   // (no cudaMalloc / cudaFree per call: cudaFree synchronises the device and
   // would serialise the contexts of a worker pool)
-  DevBuf tmp[24];
+  DevBuf tmp[32];
   // sweep configurations chosen by pcg_autotune, by decimal exponent of x
   bool tuned[64] = {};
   Tuning tuned_cfg[64];

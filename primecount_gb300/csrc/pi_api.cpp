@@ -12,6 +12,7 @@
 
 namespace pcg {
 i128 pi_any(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s, pcg_stats* st);
+i128 pi_without_d(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s, bool* needs_d);
 void pi_gourdon_terms(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s, i128 out[6]);
 int64_t phi_any(Ctx& c, int64_t x, int64_t a, const Tuning& tune, cudaStream_t s);
 }  // namespace pcg
@@ -153,6 +154,12 @@ pcg_status run_pool(size_t n, const pcg_opts* opts, const std::vector<size_t>& o
 
 extern "C" {
 
+// pi(x) of n queries.  The hard special leaves (Gourdon's D) of every query
+// with x > 1e10 run as the work items of one batched sweep on the caller's
+// context (one persistent kernel per wave over all queries' segments, the
+// waves launched as one CUDA graph), while the worker pool computes the other
+// terms of those queries and the small queries whole; each answer is then
+// the pool's part plus its D.
 pcg_status pcg_pi_batch(const pcg_i128* xs, size_t n, pcg_i128* out, const pcg_opts* opts)
 {
   if ((!xs || !out) && n) return PCG_EINVAL;
@@ -164,7 +171,60 @@ pcg_status pcg_pi_batch(const pcg_i128* xs, size_t n, pcg_i128* out, const pcg_o
     if (xs[a].hi < 0 || xs[b].hi < 0) return xs[a].hi > xs[b].hi;
     return key(a) > key(b);
   });
-  return run_pool(n, opts, order, [&](size_t i, const pcg_opts* o) { return pcg_pi(xs[i], o, &out[i]); });
+  const Tuning tune = tune_of(opts);
+  // the queries whose D joins the batched sweep
+  std::vector<int64_t> slot(n, -1);
+  std::vector<SweepProblem> pbs;
+  pcg_status st0 = pcg_guarded(opts, [&](Ctx&, cudaStream_t) {
+    for (size_t i = 0; i < n; i++) {
+      if (xs[i].hi < 0) continue;
+      const u128 x = make_u128(xs[i]);
+      if (x <= (u128) 10000000000ull) continue;
+      const GourdonParams g = gourdon_params(x, tune.alpha_y, tune.alpha_z);
+      if (g.y < g.z || x > ((u128) g.y << 62)) continue;
+      SweepProblem p;
+      p.gourdon = 1;
+      p.x = x;
+      p.y = g.y;
+      p.z = g.z;
+      p.k = g.k;
+      slot[i] = (int64_t) pbs.size();
+      pbs.push_back(p);
+    }
+  });
+  if (st0 != PCG_OK) return st0;
+  std::vector<i128> dsum;
+  pcg_status sweep_st = PCG_OK;
+  std::string sweep_msg;
+  std::thread sweeper;
+  if (!pbs.empty()) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return PCG_ENODEV; }
+    sweeper = std::thread([&, dev] {
+      cudaSetDevice(dev);
+      sweep_st = pcg_guarded(opts, [&](Ctx& c, cudaStream_t s) {
+        pcg_stats st{};
+        run_sweep_batch(c, pbs, tune, s, dsum, &st);
+        c.last = st;
+      });
+      if (sweep_st != PCG_OK) sweep_msg = pcg_last_error(opts ? opts->ctx : nullptr);
+    });
+  }
+  pcg_status pst = run_pool(n, opts, order, [&](size_t i, const pcg_opts* o) {
+    if (slot[i] < 0) return pcg_pi(xs[i], o, &out[i]);
+    return pcg_guarded(o, [&](Ctx& c, cudaStream_t s) {
+      bool needs_d = false;
+      const i128 r = pi_without_d(c, make_u128(xs[i]), tune, s, &needs_d);
+      if (!needs_d) fail(PCG_EINTERNAL, "batched pi: a query without D joined the sweep");
+      out[i] = to_pcg(r);
+    });
+  });
+  if (sweeper.joinable()) sweeper.join();
+  if (pst != PCG_OK) return pst;
+  if (sweep_st != PCG_OK) return sweep_st;
+  for (size_t i = 0; i < n; i++)
+    if (slot[i] >= 0) out[i] = to_pcg(make_i128(out[i]) + dsum[(size_t) slot[i]]);
+  return PCG_OK;
 }
 
 pcg_status pcg_phi_batch(const int64_t* x, const int64_t* a, size_t n, int64_t* out, const pcg_opts* opts)

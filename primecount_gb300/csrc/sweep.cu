@@ -33,6 +33,8 @@
 #include <cstring>
 #include <chrono>
 #include <algorithm>
+#include <atomic>
+#include <exception>
 #include <mutex>
 #include <cmath>
 #include <string>
@@ -310,30 +312,41 @@ struct LevelP {
   uint32_t fcount;    // flag 8: numbers of the segment removed at this level (PiTable formula)
 };
 
-struct SweepArgs {
+// One problem of a sweep: D (gourdon = 1), S2_hard (0) or the special leaves
+// of phi(x, a) (2).  A sweep runs the segments of one or of many problems
+// (a batch): its work items are the problems' segments one after another,
+// problem q owning the items [item0, item0 + nseg).
+struct SweepQ {
   uint64_t x_lo, x_hi;
   int64_t y, z, k, L, x_star;
-  const int64_t* seglo;  // segment s = [seglo[s], seglo[s+1])
-  int32_t words;         // bitmap words per CTA (max segment = words * 240 numbers)
-  int32_t rec_cap;       // leaf records per chunk
+  int64_t item0;         // first work item of the problem
+  const int64_t* seglo;  // its segment s = [seglo[s], seglo[s+1])
+  const uint64_t* xp_tab;   // [bglob+1][3]: x/p lo, hi, min(x/p^3, 2^63-1)
   int32_t gourdon;
   int32_t pi_sqrt;       // last level of family 1
   int32_t bglob;         // columns = bglob + 1
-  int64_t wave_first;
-  int32_t wave_len;
   int32_t pad0;
+};
+
+struct SweepArgs {
+  const SweepQ* qs;      // the problems, by item0 ascending
+  int32_t nq;
+  int32_t words;         // bitmap words per CTA (max segment = words * 240 numbers)
+  int32_t rec_cap;       // leaf records per chunk
+  int32_t wave_len;
+  int64_t wave_first;    // first work item of the wave
+  const int64_t* rowoff; // [wave_len]: first cell of the item's row in cnt / smu
   const uint32_t* primes;
   int64_t nprimes;
   const uint64_t* pitab;
   int64_t pi_max;
   const void* factor;
-  const uint64_t* xp_tab;   // [bglob+1][3]: x/p lo, hi, min(x/p^3, 2^63-1)
   const uint16_t* coprime;
   const int16_t* cindex;
   const uint64_t* finv;      // floor((2^64 - 1) / m) by factor-table index
   const uint64_t* pmagic;    // floor((2^64 - 1) / p) by prime index
-  uint32_t* cnt;            // [wave_len][bglob+1]
-  int32_t* smu;             // [wave_len][bglob+1]
+  uint32_t* cnt;            // rows of the wave's items: [rowoff[i], rowoff[i] + bglob + 1)
+  int32_t* smu;             // same cells
   int64_t* segsum;          // [wave_len]
   unsigned long long* counters;  // [0] leaves, [1] two-prime leaves, [2] levels, [3] factor entries,
                                  // [4] multiples crossed off
@@ -497,9 +510,8 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
   __shared__ long long s_red[NT / 32];
   __shared__ unsigned long long s_ctr[5];
 
+  __shared__ SweepQ s_q;                               // the problem of the current segment
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const u128 x = ((u128) A.x_hi << 64) | A.x_lo;
-  const int cols = A.bglob + 1;
   const int cap = A.rec_cap;
   const FT* __restrict__ factor = (const FT*) A.factor;
   for (int i = tid; i < 480; i += NT) cop[i] = A.coprime[i];
@@ -525,31 +537,45 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
     __syncthreads();
     const int ws = s_ws;
     if (ws >= A.wave_len) break;
-    const int64_t s = A.wave_first + ws;
-    const int64_t low = A.seglo[s];
-    const int64_t high = A.seglo[s + 1];
+    const int64_t item = A.wave_first + ws;
+    if (tid == 0) {
+      // the problem owning the item: the last with item0 <= item
+      int lo = 0, hi = A.nq - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (A.qs[mid].item0 <= item) lo = mid; else hi = mid - 1;
+      }
+      s_q = A.qs[lo];
+    }
+    __syncthreads();
+    const SweepQ& PQ = s_q;
+    const u128 x = ((u128) PQ.x_hi << 64) | PQ.x_lo;
+    const int64_t rowbase = A.rowoff[ws];
+    const int64_t s = item - PQ.item0;
+    const int64_t low = PQ.seglo[s];
+    const int64_t high = PQ.seglo[s + 1];
     const int64_t low1 = dmax(low, 1);
 
     // level bounds of this segment (chunk bounds of D.cpp:83-94 / S2_hard.cpp:64-71)
     int64_t bmin_leaf, bmax_leaf, bcnt;
-    if (A.gourdon == 2) {
+    if (PQ.gourdon == 2) {
       // phi(x, a) special leaves: p_b <= p_a (held in x_star), m <= y
-      bmax_leaf = dpi(A.pitab, (uint64_t) dmin(disqrt(div128(x, (uint64_t) low1)), A.x_star));
-      bmin_leaf = dpi(A.pitab, (uint64_t) dmin(A.L / high, A.x_star));
-      bcnt = dpi(A.pitab, (uint64_t) dmin(disqrt(div128(x, (uint64_t) high)), A.x_star));
-    } else if (A.gourdon) {
-      bmax_leaf = dpi(A.pitab, (uint64_t) dmin(dmin(disqrt(div128(x, (uint64_t) low1)), disqrt((u128) high)), A.x_star));
-      bmin_leaf = dpi(A.pitab, (uint64_t) dmin(A.L / high, A.x_star));
-      bcnt = dpi(A.pitab, (uint64_t) dmin(disqrt(div128(x, (uint64_t) high)), A.x_star));
+      bmax_leaf = dpi(A.pitab, (uint64_t) dmin(disqrt(div128(x, (uint64_t) low1)), PQ.x_star));
+      bmin_leaf = dpi(A.pitab, (uint64_t) dmin(PQ.L / high, PQ.x_star));
+      bcnt = dpi(A.pitab, (uint64_t) dmin(disqrt(div128(x, (uint64_t) high)), PQ.x_star));
+    } else if (PQ.gourdon) {
+      bmax_leaf = dpi(A.pitab, (uint64_t) dmin(dmin(disqrt(div128(x, (uint64_t) low1)), disqrt((u128) high)), PQ.x_star));
+      bmin_leaf = dpi(A.pitab, (uint64_t) dmin(PQ.L / high, PQ.x_star));
+      bcnt = dpi(A.pitab, (uint64_t) dmin(disqrt(div128(x, (uint64_t) high)), PQ.x_star));
     } else {
-      bmax_leaf = (high <= A.y) ? A.pi_sqrt
-          : dpi(A.pitab, (uint64_t) dmin(dmin(disqrt(div128(x, (uint64_t) low1)), disqrt((u128) A.z)), A.y));
+      bmax_leaf = (high <= PQ.y) ? PQ.pi_sqrt
+          : dpi(A.pitab, (uint64_t) dmin(dmin(disqrt(div128(x, (uint64_t) low1)), disqrt((u128) PQ.z)), PQ.y));
       uint64_t pmax = bmax_leaf > 0 ? A.primes[bmax_leaf] : 0;
-      bmin_leaf = dpi(A.pitab, (uint64_t) dmin(A.z / high, (int64_t) pmax));
-      bcnt = dmax(A.pi_sqrt, dpi(A.pitab, (uint64_t) dmin(dmin(disqrt(div128(x, (uint64_t) high)), disqrt((u128) A.z)), A.y)));
+      bmin_leaf = dpi(A.pitab, (uint64_t) dmin(PQ.z / high, (int64_t) pmax));
+      bcnt = dmax(PQ.pi_sqrt, dpi(A.pitab, (uint64_t) dmin(dmin(disqrt(div128(x, (uint64_t) high)), disqrt((u128) PQ.z)), PQ.y)));
     }
-    bmin_leaf = dmax(A.k, bmin_leaf) + 1;
-    const int Bs = (int) dmin(dmax(bmax_leaf, bcnt), (int64_t) A.bglob);
+    bmin_leaf = dmax(PQ.k, bmin_leaf) + 1;
+    const int Bs = (int) dmin(dmax(bmax_leaf, bcnt), (int64_t) PQ.bglob);
 
     // fill the segment: every number coprime to 30 in [low, high)
     const uint32_t span = (uint32_t) (high - low);
@@ -626,29 +652,29 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
           }
           if (p >= 64) ncross = P.jn;
           if (b >= bmin_leaf && b <= bmax_leaf) {
-            const uint64_t* xt = A.xp_tab + 3 * b;
+            const uint64_t* xt = PQ.xp_tab + 3 * b;
             const u128 xp = ((u128) xt[1] << 64) | xt[0];
             const int64_t xpp = (int64_t) xt[2];
             const int64_t prime = (int64_t) p;
             bool stop = false;
-            if (b <= A.pi_sqrt) {
+            if (b <= PQ.pi_sqrt) {
               int64_t min_m, max_m;
-              if (A.gourdon == 2) {
+              if (PQ.gourdon == 2) {
                 // phi(x, a): m in (max(y / p, x / (p high)), min(y, x / (p low))]
-                int64_t xp_high = divcap(xp, (uint64_t) high, A.y);
-                min_m = dmax(xp_high, A.y / prime);
-                max_m = divcap(xp, (uint64_t) low1, A.y);
+                int64_t xp_high = divcap(xp, (uint64_t) high, PQ.y);
+                min_m = dmax(xp_high, PQ.y / prime);
+                max_m = divcap(xp, (uint64_t) low1, PQ.y);
                 P.thr = (uint32_t) (2 * b + 1);
-              } else if (A.gourdon) {
-                int64_t xp_low = divcap(xp, (uint64_t) low1, A.z);
-                int64_t xp_high = divcap(xp, (uint64_t) high, A.z);
-                min_m = dmax(xp_high, A.z / prime);
+              } else if (PQ.gourdon) {
+                int64_t xp_low = divcap(xp, (uint64_t) low1, PQ.z);
+                int64_t xp_high = divcap(xp, (uint64_t) high, PQ.z);
+                min_m = dmax(xp_high, PQ.z / prime);
                 max_m = dmin(xpp, xp_low);
                 P.thr = (uint32_t) (2 * b + 1);
               } else {
-                int64_t xp_high = divcap(xp, (uint64_t) high, A.y);
-                min_m = dmax(xp_high, A.y / prime);
-                max_m = divcap(xp, (uint64_t) low1, A.y);
+                int64_t xp_high = divcap(xp, (uint64_t) high, PQ.y);
+                min_m = dmax(xp_high, PQ.y / prime);
+                max_m = divcap(xp, (uint64_t) low1, PQ.y);
                 P.thr = (uint32_t) prime;
               }
               if (prime >= max_m) stop = true;
@@ -658,15 +684,15 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                 if (P.hi > P.lo) P.flags |= 1;
               }
             } else {
-              int64_t xp_low = divcap(xp, (uint64_t) low1, A.y);
-              int64_t xp_high = divcap(xp, (uint64_t) high, A.y);
+              int64_t xp_low = divcap(xp, (uint64_t) low1, PQ.y);
+              int64_t xp_high = divcap(xp, (uint64_t) high, PQ.y);
               int64_t l, min_hard;
-              if (A.gourdon) {
+              if (PQ.gourdon) {
                 int64_t max_m = dmin(xpp, xp_low);
                 l = dpi(A.pitab, (uint64_t) max_m);
                 min_hard = dmax(xp_high, prime);
               } else {
-                l = dpi(A.pitab, (uint64_t) dmin(xp_low, A.z / prime));
+                l = dpi(A.pitab, (uint64_t) dmin(xp_low, PQ.z / prime));
                 min_hard = dmax(xp_high, prime);
               }
               if (prime >= (int64_t) A.primes[l]) stop = true;
@@ -741,7 +767,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
           const int64_t hi0 = Q.hi - (w0 - loff[li]);        // table index of entry f is hi0 - f
           const bool two = (Q.flags & 2) != 0;
           const uint32_t thr = Q.thr;
-          const uint64_t* xt = A.xp_tab + 3 * (int64_t) Q.level;
+          const uint64_t* xt = PQ.xp_tab + 3 * (int64_t) Q.level;
           const uint64_t xlo = xt[0], xhi = xt[1];
           unsigned nl = 0;
           if (compact && hi0 < 0x7FFFFFFFll) {
@@ -954,7 +980,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                 const LevelP& Q = lp[jl[u]];
                 uint32_t r = REC_NONE;
                 if (mdiv[u]) {
-                  const uint64_t nn = (Q.flags & 16) ? div_xp(Q.xlo, A.xp_tab[3 * (int64_t) Q.level + 1], mdiv[u])
+                  const uint64_t nn = (Q.flags & 16) ? div_xp(Q.xlo, PQ.xp_tab[3 * (int64_t) Q.level + 1], mdiv[u])
                                                      : div_magic(Q.xlo, mdiv[u], minv[u]);
                   r = (uint32_t) (nn - (uint64_t) low);
                   if (!(Q.flags & 2) && !(fv[u] & 1)) r |= 1u << 30;
@@ -984,7 +1010,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
             // counts from the prefix, all their multiples crossed off at once
             const int64_t r0 = rpre[li];
             for (int t = tid; t < re - li; t += NT)
-              A.cnt[(int64_t) ws * cols + b0 + li + t] = total - (uint32_t) (rpre[li + t] - r0);
+              A.cnt[rowbase + b0 + li + t] = total - (uint32_t) (rpre[li + t] - r0);
             const int64_t h0 = hoff[li], h1 = hoff[re];
             for (int64_t h = h0 + tid; h < h1; h += NT) {
               int lo = li, hi = re - 1;       // last level with hoff <= h
@@ -1113,7 +1139,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
               // the levels' counts C(s, b) and signed leaf counts M(s, b)
               const int64_t r0 = rpre[li];
               for (int t = tid; t < lj - li; t += NT) {
-                const int64_t cell = (int64_t) ws * cols + b0 + li + t;
+                const int64_t cell = rowbase + b0 + li + t;
                 A.cnt[cell] = total - (uint32_t) (rpre[li + t] - r0);
                 if (s_gsmu[t]) A.smu[cell] = s_gsmu[t];
               }
@@ -1142,7 +1168,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
           const int64_t la = loff[li], lz = loff[li + 1];
           if (lz > la && la >= wend) break;               // records start in a later window
           const int l = b0 + li;
-          if (la >= w0 && tid == 0) A.cnt[(int64_t) ws * cols + l] = total;
+          if (la >= w0 && tid == 0) A.cnt[rowbase + l] = total;
           const int ra = (int) (dmax(la, w0) - w0);
           const int rz = (int) (dmin(lz, wend) - w0);           // end of the level's window records
           const int rb = li == clev ? s_ncomp[win & 1] : rz;   // end of those still to answer
@@ -1190,7 +1216,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
             }
             __syncthreads();
           }
-          if (rz > ra && lz <= wend && tid == 0) { A.smu[(int64_t) ws * cols + l] = s_smu; s_smu = 0; }
+          if (rz > ra && lz <= wend && tid == 0) { A.smu[rowbase + l] = s_smu; s_smu = 0; }
           if (lz > wend) break;                            // the level continues in the next window
           // ---- cross off p_l and its multiples, count the numbers removed first
           const LevelP& P = lp[li];
@@ -1279,30 +1305,56 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
 }
 
 // ---- phi offsets: acc[b] += sum_s M(s, b) * sum_{s'<s} C(s', b), in segment order.
-// A block takes 32 levels; its COMBINE_WARPS warps take consecutive runs of the wave's
-// segments and sum them from a local count of 0, then the runs are chained:
-// a run k whose segments see the count R_k + r (r its local prefix) adds
-// a_k + ms_k R_k, with a_k = sum M r and ms_k = sum M over the run.
+// One block per job.  A level job takes 32 levels of one problem; its
+// COMBINE_WARPS warps take consecutive runs of the problem's items in the
+// wave and sum them from a local count of 0, then the runs are chained: a
+// run k whose segments see the count R_k + r (r its local prefix) adds
+// a_k + ms_k R_k, with a_k = sum M r and ms_k = sum M over the run.  A sum
+// job (slab < 0) adds the items' local leaf sums into the problem's column 0
+// (never a level: level jobs leave it alone).
 #define COMBINE_WARPS 16
+struct CombineJob {
+  int64_t colbase;   // the problem's first cell in run / acc / msum
+  int32_t item0;     // its first item in the wave (wave-local)
+  int32_t n;         // its items in the wave
+  int32_t cols;      // its columns (levels 0 .. cols - 1)
+  int32_t slab;      // levels [32 slab, 32 slab + 32); < 0: the local sums
+};
+
 __global__ void __launch_bounds__(32 * COMBINE_WARPS)
-k_combine(const uint32_t* __restrict__ cnt, const int32_t* __restrict__ smu, int wave_len, int cols,
-          int64_t* __restrict__ run, i128* __restrict__ acc, int64_t* __restrict__ msum)
+k_combine(const uint32_t* __restrict__ cnt, const int32_t* __restrict__ smu, const int64_t* __restrict__ rowoff,
+          const int64_t* __restrict__ segsum, const CombineJob* __restrict__ jobs, int64_t* __restrict__ run,
+          i128* __restrict__ acc, int64_t* __restrict__ msum)
 {
   __shared__ i128 s_a[COMBINE_WARPS][32];
   __shared__ long long s_m[COMBINE_WARPS][32], s_c[COMBINE_WARPS][32];
+  const CombineJob J = jobs[blockIdx.x];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int b = blockIdx.x * 32 + lane;
-  const int per = (wave_len + COMBINE_WARPS - 1) / COMBINE_WARPS;
-  const int s0 = min(wave_len, w * per), s1 = min(wave_len, s0 + per);
+  if (J.slab < 0) {
+    // per-thread partial sums fit int64 (each segment's sum does, n is small)
+    long long v = 0;
+    for (int i = threadIdx.x; i < J.n; i += blockDim.x) v += segsum[J.item0 + i];
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
+    if (lane == 0) s_m[w][0] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      i128 t = 0;
+      for (int i = 0; i < COMBINE_WARPS; i++) t += s_m[i][0];
+      acc[J.colbase] += t;
+    }
+    return;
+  }
+  const int b = J.slab * 32 + lane;
+  const int per = (J.n + COMBINE_WARPS - 1) / COMBINE_WARPS;
+  const int s0 = J.item0 + min(J.n, w * per), s1 = J.item0 + min(J.n, w * per + per);
   i128 a = 0;
   long long ms = 0, r = 0;
-  if (b < cols) {
+  if (b < J.cols) {
     int s = s0;
     for (; s + 4 <= s1; s += 4) {
-      const int32_t m0 = smu[(int64_t) s * cols + b], m1 = smu[(int64_t) (s + 1) * cols + b];
-      const int32_t m2 = smu[(int64_t) (s + 2) * cols + b], m3 = smu[(int64_t) (s + 3) * cols + b];
-      const uint32_t c0 = cnt[(int64_t) s * cols + b], c1 = cnt[(int64_t) (s + 1) * cols + b];
-      const uint32_t c2 = cnt[(int64_t) (s + 2) * cols + b], c3 = cnt[(int64_t) (s + 3) * cols + b];
+      const int64_t o0 = rowoff[s] + b, o1 = rowoff[s + 1] + b, o2 = rowoff[s + 2] + b, o3 = rowoff[s + 3] + b;
+      const int32_t m0 = smu[o0], m1 = smu[o1], m2 = smu[o2], m3 = smu[o3];
+      const uint32_t c0 = cnt[o0], c1 = cnt[o1], c2 = cnt[o2], c3 = cnt[o3];
       a += (i128) m0 * r; r += c0;
       a += (i128) m1 * r; r += c1;
       a += (i128) m2 * r; r += c2;
@@ -1310,45 +1362,29 @@ k_combine(const uint32_t* __restrict__ cnt, const int32_t* __restrict__ smu, int
       ms += (long long) m0 + m1 + m2 + m3;
     }
     for (; s < s1; s++) {
-      const int32_t m = smu[(int64_t) s * cols + b];
+      const int64_t o = rowoff[s] + b;
+      const int32_t m = smu[o];
       a += (i128) m * r;
       ms += m;
-      r += cnt[(int64_t) s * cols + b];
+      r += cnt[o];
     }
   }
   s_a[w][lane] = a;
   s_m[w][lane] = ms;
   s_c[w][lane] = r;
   __syncthreads();
-  if (w == 0 && b < cols) {
-    long long R = run[b], M = 0;
+  if (w == 0 && b < J.cols && b > 0) {
+    const int64_t cb = J.colbase + b;
+    long long R = run[cb], M = 0;
     i128 A = 0;
     for (int k = 0; k < COMBINE_WARPS; k++) {
       A += s_a[k][lane] + (i128) s_m[k][lane] * R;
       R += s_c[k][lane];
       M += s_m[k][lane];
     }
-    run[b] = R;
-    acc[b] += A;
-    if (msum) msum[b] += M;
-  }
-}
-
-// ---- local leaf sums of a wave into acc[0] (column 0 is never a level)
-__global__ void k_segsum(const int64_t* __restrict__ segsum, int n, i128* __restrict__ acc)
-{
-  __shared__ long long red[32];
-  i128 t = 0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) t += segsum[i];
-  // per-thread partial sums fit int64 (each segment's sum does, n is small)
-  long long v = (long long) t;
-  for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xffffffffu, v, d);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    i128 s = 0;
-    for (int i = 0; i < (int) (blockDim.x >> 5); i++) s += red[i];
-    acc[0] += s;
+    run[cb] = R;
+    acc[cb] += A;
+    if (msum) msum[cb] += M;
   }
 }
 
@@ -1622,6 +1658,15 @@ void ensure_factor_dr(Ctx& c, int64_t y, cudaStream_t s)
   t.build_ms += now_ms() - t0;
 }
 
+// Combine jobs of n consecutive items (wave-local item0) of one problem with
+// cols columns whose cells start at colbase: one job per 32 levels and one
+// for the local sums.
+static void add_combine_jobs(std::vector<CombineJob>& jobs, int64_t colbase, int item0, int n, int cols)
+{
+  for (int sl = 0; sl * 32 < cols; sl++) jobs.push_back(CombineJob{colbase, item0, n, cols, sl});
+  jobs.push_back(CombineJob{colbase, item0, n, cols, -1});
+}
+
 template <typename FT, int NT>
 static void set_sweep_attr(size_t smem)
 {
@@ -1653,17 +1698,18 @@ static void launch_sweep(const SweepArgs& a, int grid, size_t smem, cudaStream_t
 // dens[b] = 0.56 / log(p_b) for b in [1, bglob].  The grid cells are costed
 // on nth host threads (1: the calling thread only, no thread is created).
 // Each segment end is passed to push(end) in order, starting with 0; a push
-// returning false stops the plan (the return value is then false).
+// returning false stops the plan (the return value is then false).  G grid
+// cells (at most PLAN_GRID).
 #define PLAN_GRID 1200
 template <class Push>
 static bool plan_segments_core(const SweepProblem& pb, const Tables& t, int64_t L, int64_t x_star,
                                int64_t pi_sqrt, int64_t bglob, int64_t smax, int grid, const double* dens,
-                               unsigned nth, Push push)
+                               unsigned nth, Push push, int G = PLAN_GRID)
 {
   const double x = (double) pb.x;
   const double y = (double) pb.y, z = (double) pb.z;
-  const int G = PLAN_GRID;
-  double g[G + 1], cost[G], cum[G + 1];
+  G = std::max(2, std::min(G, PLAN_GRID));
+  double g[PLAN_GRID + 1], cost[PLAN_GRID], cum[PLAN_GRID + 1];
   g[0] = 0;
   const double a0 = 240;
   const double ratio = std::pow((double) L / a0, 1.0 / (G - 1));
@@ -1968,27 +2014,45 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune_in, cud
   unsigned long long* d_counters = (unsigned long long*) c.misc.p;
   int* d_queue = (int*) ((char*) c.misc.p + 256);   // after the 32 counters
 
+  // the problem, the row offsets of a wave's items and the combine jobs of a
+  // full wave and of the last (shorter) one
+  SweepQ q0;
+  memset(&q0, 0, sizeof(q0));
+  q0.x_lo = (uint64_t) x;
+  q0.x_hi = (uint64_t) (x >> 64);
+  q0.y = pb.y;
+  q0.z = pb.z;
+  q0.k = pb.k;
+  q0.L = L;
+  q0.x_star = x_star;
+  q0.item0 = 0;
+  q0.seglo = segbuf.as<int64_t>();
+  q0.xp_tab = d_xp;
+  q0.gourdon = pb.gourdon;
+  q0.pi_sqrt = (int) pi_sqrt;
+  q0.bglob = (int) bglob;
+  std::vector<int64_t> rowoff((size_t) wave_len);
+  for (int64_t i = 0; i < wave_len; i++) rowoff[(size_t) i] = i * cols;
+  DevBuf& qbuf = c.tmp[T_SW_Q];
+  DevBuf& rowbuf = c.tmp[T_SW_ROW];
+  DevBuf& jobbuf = c.tmp[T_SW_JOB];
+  qbuf.alloc(sizeof(SweepQ));
+  rowbuf.alloc(rowoff.size() * 8);
+  PCG_CUDA(cudaMemcpyAsync(qbuf.p, &q0, sizeof(SweepQ), cudaMemcpyHostToDevice, s));
+  PCG_CUDA(cudaMemcpyAsync(rowbuf.p, rowoff.data(), rowoff.size() * 8, cudaMemcpyHostToDevice, s));
+
   SweepArgs a;
   memset(&a, 0, sizeof(a));
-  a.x_lo = (uint64_t) x;
-  a.x_hi = (uint64_t) (x >> 64);
-  a.y = pb.y;
-  a.z = pb.z;
-  a.k = pb.k;
-  a.L = L;
-  a.x_star = x_star;
-  a.seglo = segbuf.as<int64_t>();
+  a.qs = qbuf.as<SweepQ>();
+  a.nq = 1;
+  a.rowoff = rowbuf.as<int64_t>();
   a.words = words;
   a.rec_cap = cap;
-  a.gourdon = pb.gourdon;
-  a.pi_sqrt = (int) pi_sqrt;
-  a.bglob = (int) bglob;
   a.primes = c.tab.primes.as<uint32_t>();
   a.nprimes = c.tab.nprimes;
   a.pitab = c.tab.pitab.as<uint64_t>();
   a.pi_max = c.tab.prime_limit;
   a.factor = pb.gourdon ? c.tab.factor_d.p : c.tab.factor_dr.p;
-  a.xp_tab = d_xp;
   a.coprime = c.tab.coprime.as<uint16_t>();
   a.group_max = tune.group >= 0 ? std::min(tune.group, GROUP_MAX) : sweep_group_max();
   a.cindex = c.tab.cindex.as<int16_t>();
@@ -2048,6 +2112,15 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune_in, cud
     last_write = now_ms();
   };
 
+  // combine jobs of a full wave and of the last one (from start_first on)
+  const int64_t last_len = seg_end > start_first ? (seg_end - start_first - 1) % wave_len + 1 : wave_len;
+  std::vector<CombineJob> jobs;
+  add_combine_jobs(jobs, 0, 0, (int) wave_len, cols);
+  const int njobs = (int) jobs.size();
+  add_combine_jobs(jobs, 0, 0, (int) last_len, cols);
+  jobbuf.alloc(jobs.size() * sizeof(CombineJob));
+  PCG_CUDA(cudaMemcpyAsync(jobbuf.p, jobs.data(), jobs.size() * sizeof(CombineJob), cudaMemcpyHostToDevice, s));
+
   PCG_CUDA(cudaEventRecord(c.ev[0], s));
   uint64_t launches = 0;
   float ms_sweep = 0;
@@ -2072,11 +2145,11 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune_in, cud
     else { if (fbytes == 2) launch_sweep<uint16_t, 128>(a, g, smem, s); else launch_sweep<uint32_t, 128>(a, g, smem, s); }
     PCG_CUDA(cudaGetLastError());
     PCG_CUDA(cudaEventRecord(c.kev[2 * waves + 1], s));
-    k_combine<<<(cols + 31) / 32, 32 * COMBINE_WARPS, 0, s>>>(a.cnt, a.smu, wl, cols, c.run.as<int64_t>(),
-                                                             c.acc.as<i128>(), c.msum.as<int64_t>());
-    k_segsum<<<1, 1024, 0, s>>>(a.segsum, wl, c.acc.as<i128>());
+    const CombineJob* wj = jobbuf.as<CombineJob>() + (wl == wave_len ? 0 : njobs);
+    k_combine<<<njobs, 32 * COMBINE_WARPS, 0, s>>>(a.cnt, a.smu, a.rowoff, a.segsum, wj, c.run.as<int64_t>(),
+                                                  c.acc.as<i128>(), c.msum.as<int64_t>());
     PCG_CUDA(cudaGetLastError());
-    launches += 3;
+    launches += 2;
     waves++;
     ck.waves++;
     const int64_t next = std::min<int64_t>(first + wave_len, seg_end);
@@ -2110,7 +2183,8 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune_in, cud
   }
   st.sweep_kernel_ms = kms;
   st.sweep_launches = (uint64_t) waves;
-  st.h2d_bytes = xp.size() * 8 + seglo.size() * 8;
+  st.h2d_bytes = xp.size() * 8 + seglo.size() * 8 + sizeof(SweepQ) + rowoff.size() * 8 +
+                 jobs.size() * sizeof(CombineJob);
   st.d2h_bytes = (uint64_t) cols * 16 + sizeof(ctr);
   i128 sum = 0;
   for (int b = 0; b < cols; b++) sum += acc[(size_t) b];
@@ -2133,6 +2207,371 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune_in, cud
 }
 
 
+// Device working memory of one sweep over [0, L) with cols columns, at the
+// default launch shape (words per segment, 2 CTAs per SM): the count and sign
+// rows of a wave, the segment, x / p, row and job tables and the sums.  The
+// segment planner cuts at most about L / (words * 240) + 6 grid segments.
+uint64_t sweep_device_bytes(int num_sms, int64_t L, int64_t cols, int words)
+{
+  if (L <= 0 || cols <= 1) return 0;
+  const int64_t grid = (int64_t) num_sms * 2;
+  const int64_t nseg = L / ((int64_t) words * 240) + 6 * grid + 2;
+  const int64_t max_rows = std::max<int64_t>(1, (int64_t) (1ull << 30) / (cols * 8));
+  const int64_t wave = std::max<int64_t>(1, std::min<int64_t>({nseg, grid * 8, max_rows}));
+  return (uint64_t) (wave * cols * 8 + wave * 16 + (nseg + 1) * 8 + cols * 56 +
+                     ((cols + 31) / 32 + 1) * 2 * (int64_t) sizeof(CombineJob) + 4096 + sizeof(SweepQ));
+}
+
+// The per-call working memory a context keeps between calls (count and sign
+// rows, per-call temporaries), freed; the resident tables stay.
+uint64_t ctx_trim(Ctx& c)
+{
+  uint64_t freed = c.cnt.bytes + c.smu.bytes + c.segsum.bytes + c.run.bytes + c.acc.bytes + c.msum.bytes;
+  c.cnt.free_();
+  c.smu.free_();
+  c.segsum.free_();
+  c.run.free_();
+  c.acc.free_();
+  c.msum.free_();
+  for (DevBuf& b : c.tmp) {
+    freed += b.bytes;
+    b.free_();
+  }
+  return freed;
+}
+
+// ================================================================ batched sweep
+// D(x, y, z, k) of many problems in one sweep.  Every problem's segments are
+// the work items of one persistent kernel launch per wave (CTAs pull items
+// of all problems from one atomic counter); a wave is a run of consecutive
+// items whose count and sign rows fit the budget, and its combine jobs scan
+// each problem's items in order.  The whole launch sequence is captured in a
+// CUDA graph and launched once.  The tables are shared: primes and PiTable up
+// to the largest y, one FactorTableD for the largest z built without the
+// mpf <= y filter -- exact for problems with y >= z, whose filter passes
+// every n <= z (the reference's default parameters have y = z).
+void run_sweep_batch(Ctx& c, const std::vector<SweepProblem>& pbs, const Tuning& tune_in, cudaStream_t s,
+                     std::vector<i128>& sums, pcg_stats* stp)
+{
+  pcg_stats st{};
+  const double t_start = now_ms();
+  c.tab.build_ms = 0;
+  const size_t nq = pbs.size();
+  sums.assign(nq, 0);
+  if (nq == 0) { if (stp) *stp = st; return; }
+  int64_t ymax = 1, zmax = 1;
+  u128 xmax = 0;
+  for (const SweepProblem& p : pbs) {
+    if (p.gourdon != 1 || p.y < p.z || p.y < 1 || p.z < 1) fail(PCG_EINVAL, "batched sweep: D problems with y >= z only");
+    ymax = std::max(ymax, p.y);
+    zmax = std::max(zmax, p.z);
+    xmax = std::max(xmax, p.x);
+  }
+  ensure_prime_tables(c, ymax, s);
+  ensure_factor_d(c, zmax, zmax, s);
+  const Tables& T = c.tab;
+  st.table_ms = T.build_ms;
+
+  // tuning: the context's autotuned choice for the largest x's decade, else the defaults
+  Tuning tune = tune_in;
+  {
+    const int e = (int) std::floor(std::log10((double) xmax));
+    if (e >= 0 && e < 64 && c.tuned[e] && !tune.segment_words && !tune.cta_threads && !tune.ctas_per_sm &&
+        tune.group < 0) {
+      tune.segment_words = c.tuned_cfg[e].segment_words;
+      tune.cta_threads = c.tuned_cfg[e].cta_threads;
+      tune.ctas_per_sm = c.tuned_cfg[e].ctas_per_sm;
+      tune.group = c.tuned_cfg[e].group;
+    }
+  }
+  const int NT = (tune.cta_threads == 512 || tune.cta_threads == 128) ? tune.cta_threads : 256;
+  int words = tune.segment_words > 0 ? tune.segment_words : 8192;
+  const int wq = std::max(8 * NT, 2048);
+  words = std::max(words, wq);
+  words = (words + wq - 1) / wq * wq;
+  const int cap = 3584;
+  const size_t smem = (size_t) words * 8 + PAT_WORDS * 8 + (size_t) (NT + 1) * 8 * 3 + (size_t) (words / 8) * 8 +
+                      sizeof(LevelP) * NT + (size_t) cap * 4 + (size_t) NT * 2 + 480 * 2 + (size_t) NT * 4 + 32;
+  if (smem > c.smem_optin) fail(PCG_EINVAL, "segment too large for shared memory");
+  const int fbytes = T.fd_bytes;
+  int occ = 0;
+  if (NT == 512) { if (fbytes == 2) occupancy_sweep<uint16_t, 512>(&occ, smem); else occupancy_sweep<uint32_t, 512>(&occ, smem); }
+  else if (NT == 256) { if (fbytes == 2) occupancy_sweep<uint16_t, 256>(&occ, smem); else occupancy_sweep<uint32_t, 256>(&occ, smem); }
+  else { if (fbytes == 2) occupancy_sweep<uint16_t, 128>(&occ, smem); else occupancy_sweep<uint32_t, 128>(&occ, smem); }
+  const int ctas = tune.ctas_per_sm > 0 ? std::min(tune.ctas_per_sm, std::max(occ, 1)) : std::max(occ, 1);
+  const int grid = c.num_sms * ctas;
+  const int64_t smax = (int64_t) words * 240;
+
+  // per problem: parameters, x / p table and segment plan (host threads)
+  struct Plan {
+    SweepQ q;
+    std::vector<uint64_t> xp;
+    std::vector<int64_t> seg;
+    int64_t cols = 0;
+  };
+  std::vector<Plan> plans(nq);
+  {
+    std::vector<double> dens((size_t) host_pi(T, (uint64_t) std::min<int64_t>(ymax, T.prime_limit)) + 2, 0.0);
+    for (size_t b = 1; b < dens.size() && (int64_t) b <= T.nprimes; b++)
+      dens[b] = 0.56 / std::log(std::max((double) T.h_primes[b], 3.0));
+    std::atomic<size_t> next{0};
+    std::exception_ptr err;
+    std::mutex err_mu;
+    auto work = [&] {
+      for (;;) {
+        const size_t i = next.fetch_add(1);
+        if (i >= nq) return;
+        try {
+          const SweepProblem& pb = pbs[i];
+          Plan& P = plans[i];
+          memset(&P.q, 0, sizeof(P.q));
+          const u128 x = pb.x;
+          const int64_t L = (int64_t) (x / (u128) pb.z);
+          const int64_t x_star = x_star_gourdon(x, pb.y);
+          const int64_t pi_sqrt = host_pi(T, (uint64_t) isqrt((u128) pb.z));
+          const int64_t bglob = host_pi(T, (uint64_t) x_star);
+          if (L <= 0 || bglob < 1) continue;
+          P.cols = bglob + 1;
+          P.xp.assign((size_t) P.cols * 3, 0);
+          for (int64_t b = 1; b <= bglob; b++) {
+            const u128 p = T.h_primes[(size_t) b];
+            const u128 q = x / p, q3 = q / (p * p);
+            P.xp[3 * b] = (uint64_t) q;
+            P.xp[3 * b + 1] = (uint64_t) (q >> 64);
+            P.xp[3 * b + 2] = q3 > (u128) INT64_MAX ? (uint64_t) INT64_MAX : (uint64_t) q3;
+          }
+          // small problems: one cost cell per segment is plenty
+          const int G = (int) std::min<int64_t>(PLAN_GRID, std::max<int64_t>(16, 4 * (L / smax + 1)));
+          plan_segments_core(pb, T, L, x_star, pi_sqrt, bglob, smax, grid, dens.data(), 1,
+                             [&](int64_t v) { P.seg.push_back(v); return true; }, G);
+          P.q.x_lo = (uint64_t) x;
+          P.q.x_hi = (uint64_t) (x >> 64);
+          P.q.y = pb.y;
+          P.q.z = pb.z;
+          P.q.k = pb.k;
+          P.q.L = L;
+          P.q.x_star = x_star;
+          P.q.gourdon = 1;
+          P.q.pi_sqrt = (int) pi_sqrt;
+          P.q.bglob = (int) bglob;
+        } catch (...) {
+          std::lock_guard<std::mutex> g(err_mu);
+          if (!err) err = std::current_exception();
+          return;
+        }
+      }
+    };
+    const unsigned nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> th;
+    for (unsigned k = 0; k < nth; k++) th.emplace_back(work);
+    for (auto& h : th) h.join();
+    if (err) std::rethrow_exception(err);
+  }
+
+  // concatenated problem tables; items numbered problem by problem
+  std::vector<size_t> live;
+  int64_t nitems = 0, ncells = 0, nseg_all = 0, nxp = 0;
+  for (size_t i = 0; i < nq; i++) {
+    if (plans[i].cols == 0) continue;
+    live.push_back(i);
+    nseg_all += (int64_t) plans[i].seg.size();
+    nxp += (int64_t) plans[i].xp.size();
+    ncells += plans[i].cols;
+    nitems += (int64_t) plans[i].seg.size() - 1;
+  }
+  if (live.empty()) { st.total_ms = now_ms() - t_start; if (stp) *stp = st; return; }
+  std::vector<int64_t> seg_all;
+  std::vector<uint64_t> xp_all;
+  seg_all.reserve((size_t) nseg_all);
+  xp_all.reserve((size_t) nxp);
+  DevBuf& segbuf = c.tmp[T_SW_SEG];
+  DevBuf& xpbuf = c.tmp[T_SW_XP];
+  segbuf.alloc((size_t) nseg_all * 8);
+  xpbuf.alloc((size_t) nxp * 8);
+  std::vector<SweepQ> qs;
+  std::vector<int64_t> colbase;   // by live index
+  std::vector<int64_t> first_item;
+  {
+    int64_t item = 0, cb = 0;
+    for (size_t li = 0; li < live.size(); li++) {
+      Plan& P = plans[live[li]];
+      P.q.item0 = item;
+      P.q.seglo = segbuf.as<int64_t>() + seg_all.size();
+      P.q.xp_tab = xpbuf.as<uint64_t>() + xp_all.size();
+      seg_all.insert(seg_all.end(), P.seg.begin(), P.seg.end());
+      xp_all.insert(xp_all.end(), P.xp.begin(), P.xp.end());
+      qs.push_back(P.q);
+      colbase.push_back(cb);
+      first_item.push_back(item);
+      item += (int64_t) P.seg.size() - 1;
+      cb += P.cols;
+    }
+  }
+  // waves: consecutive items whose rows fit the budget; per wave the items'
+  // row offsets and the combine jobs of each problem run in it
+  const int64_t cell_budget = (int64_t) (1ull << 30) / 8;
+  const int64_t item_cap = (int64_t) grid * 16;
+  struct Wave { int64_t first, len, row_at, job_at, njobs, cells; };
+  std::vector<Wave> waves;
+  std::vector<int64_t> rows;
+  std::vector<CombineJob> jobs;
+  {
+    size_t li = 0;
+    int64_t item = 0;
+    while (item < nitems) {
+      Wave w{item, 0, (int64_t) rows.size(), (int64_t) jobs.size(), 0, 0};
+      while (item < nitems) {
+        while (li + 1 < live.size() && first_item[li + 1] <= item) li++;
+        const int64_t cols = plans[live[li]].cols;
+        if (w.len > 0 && (w.len >= item_cap || w.cells + cols > cell_budget)) break;
+        rows.push_back(w.cells);
+        w.cells += cols;
+        w.len++;
+        item++;
+      }
+      // jobs: the runs of each problem's items inside the wave
+      int64_t i = w.first;
+      size_t lj = 0;
+      while (lj + 1 < live.size() && first_item[lj + 1] <= i) lj++;
+      while (i < w.first + w.len) {
+        const int64_t pend = (lj + 1 < live.size()) ? first_item[lj + 1] : nitems;
+        const int64_t e = std::min(pend, w.first + w.len);
+        add_combine_jobs(jobs, colbase[lj], (int) (i - w.first), (int) (e - i), (int) plans[live[lj]].cols);
+        i = e;
+        lj++;
+      }
+      w.njobs = (int64_t) jobs.size() - w.job_at;
+      waves.push_back(w);
+    }
+  }
+  int64_t max_cells = 0, max_len = 0;
+  for (const Wave& w : waves) { max_cells = std::max(max_cells, w.cells); max_len = std::max(max_len, w.len); }
+
+  DevBuf& qbuf = c.tmp[T_SW_Q];
+  DevBuf& rowbuf = c.tmp[T_SW_ROW];
+  DevBuf& jobbuf = c.tmp[T_SW_JOB];
+  qbuf.alloc(qs.size() * sizeof(SweepQ));
+  rowbuf.alloc(rows.size() * 8);
+  jobbuf.alloc(jobs.size() * sizeof(CombineJob));
+  c.cnt.alloc((size_t) max_cells * 4);
+  c.smu.alloc((size_t) max_cells * 4);
+  c.segsum.alloc((size_t) max_len * 8);
+  c.run.alloc((size_t) ncells * 8);
+  c.acc.alloc((size_t) ncells * 16);
+  c.misc.alloc(4096);
+  PCG_CUDA(cudaMemcpyAsync(segbuf.p, seg_all.data(), seg_all.size() * 8, cudaMemcpyHostToDevice, s));
+  PCG_CUDA(cudaMemcpyAsync(xpbuf.p, xp_all.data(), xp_all.size() * 8, cudaMemcpyHostToDevice, s));
+  PCG_CUDA(cudaMemcpyAsync(qbuf.p, qs.data(), qs.size() * sizeof(SweepQ), cudaMemcpyHostToDevice, s));
+  PCG_CUDA(cudaMemcpyAsync(rowbuf.p, rows.data(), rows.size() * 8, cudaMemcpyHostToDevice, s));
+  PCG_CUDA(cudaMemcpyAsync(jobbuf.p, jobs.data(), jobs.size() * sizeof(CombineJob), cudaMemcpyHostToDevice, s));
+  PCG_CUDA(cudaMemsetAsync(c.run.p, 0, (size_t) ncells * 8, s));
+  PCG_CUDA(cudaMemsetAsync(c.acc.p, 0, (size_t) ncells * 16, s));
+  PCG_CUDA(cudaMemsetAsync(c.misc.p, 0, 4096, s));
+  unsigned long long* d_counters = (unsigned long long*) c.misc.p;
+  int* d_queue = (int*) ((char*) c.misc.p + 256);
+  // the launch attributes are set before the capture
+  if (NT == 512) { if (fbytes == 2) set_sweep_attr<uint16_t, 512>(smem); else set_sweep_attr<uint32_t, 512>(smem); }
+  else if (NT == 256) { if (fbytes == 2) set_sweep_attr<uint16_t, 256>(smem); else set_sweep_attr<uint32_t, 256>(smem); }
+  else { if (fbytes == 2) set_sweep_attr<uint16_t, 128>(smem); else set_sweep_attr<uint32_t, 128>(smem); }
+  PCG_CUDA(cudaStreamSynchronize(s));
+
+  SweepArgs a;
+  memset(&a, 0, sizeof(a));
+  a.qs = qbuf.as<SweepQ>();
+  a.nq = (int) qs.size();
+  a.words = words;
+  a.rec_cap = cap;
+  a.primes = T.primes.as<uint32_t>();
+  a.nprimes = T.nprimes;
+  a.pitab = T.pitab.as<uint64_t>();
+  a.pi_max = T.prime_limit;
+  a.factor = T.factor_d.p;
+  a.coprime = T.coprime.as<uint16_t>();
+  a.group_max = tune.group >= 0 ? std::min(tune.group, GROUP_MAX) : sweep_group_max();
+  a.cindex = T.cindex.as<int16_t>();
+  a.finv = T.finv.as<uint64_t>();
+  a.pmagic = T.pmagic.as<uint64_t>();
+  a.cnt = c.cnt.as<uint32_t>();
+  a.smu = c.smu.as<int32_t>();
+  a.segsum = c.segsum.as<int64_t>();
+  a.counters = d_counters;
+
+  // the wave sequence, captured into one graph
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  PCG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  try {
+    for (size_t wi = 0; wi < waves.size(); wi++) {
+      const Wave& w = waves[wi];
+      a.wave_first = w.first;
+      a.wave_len = (int32_t) w.len;
+      a.rowoff = rowbuf.as<int64_t>() + w.row_at;
+      a.queue = d_queue + (wi % 16);
+      PCG_CUDA(cudaMemsetAsync(c.cnt.p, 0, (size_t) w.cells * 4, s));
+      PCG_CUDA(cudaMemsetAsync(c.smu.p, 0, (size_t) w.cells * 4, s));
+      if (wi % 16 == 0 && wi > 0) PCG_CUDA(cudaMemsetAsync(d_queue, 0, 64, s));
+      const int g = (int) std::min<int64_t>(grid, w.len);
+      if (NT == 512) { if (fbytes == 2) k_sweep<uint16_t, 512><<<g, 512, smem, s>>>(a); else k_sweep<uint32_t, 512><<<g, 512, smem, s>>>(a); }
+      else if (NT == 256) { if (fbytes == 2) k_sweep<uint16_t, 256><<<g, 256, smem, s>>>(a); else k_sweep<uint32_t, 256><<<g, 256, smem, s>>>(a); }
+      else { if (fbytes == 2) k_sweep<uint16_t, 128><<<g, 128, smem, s>>>(a); else k_sweep<uint32_t, 128><<<g, 128, smem, s>>>(a); }
+      PCG_CUDA(cudaGetLastError());
+      k_combine<<<(unsigned) w.njobs, 32 * COMBINE_WARPS, 0, s>>>(a.cnt, a.smu, a.rowoff, a.segsum,
+                                                                  jobbuf.as<CombineJob>() + w.job_at, c.run.as<int64_t>(),
+                                                                  c.acc.as<i128>(), nullptr);
+      PCG_CUDA(cudaGetLastError());
+    }
+    PCG_CUDA(cudaStreamEndCapture(s, &graph));
+  } catch (...) {
+    cudaGraph_t g2 = nullptr;
+    cudaStreamEndCapture(s, &g2);
+    if (g2) cudaGraphDestroy(g2);
+    cudaGetLastError();
+    throw;
+  }
+  try {
+    PCG_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+    PCG_CUDA(cudaEventRecord(c.ev[0], s));
+    PCG_CUDA(cudaGraphLaunch(exec, s));
+    PCG_CUDA(cudaEventRecord(c.ev[1], s));
+    std::vector<i128> acc((size_t) ncells);
+    unsigned long long ctr[5];
+    PCG_CUDA(cudaMemcpyAsync(acc.data(), c.acc.p, (size_t) ncells * 16, cudaMemcpyDeviceToHost, s));
+    PCG_CUDA(cudaMemcpyAsync(ctr, d_counters, sizeof(ctr), cudaMemcpyDeviceToHost, s));
+    PCG_CUDA(cudaStreamSynchronize(s));
+    for (size_t li = 0; li < live.size(); li++) {
+      i128 t = 0;
+      for (int64_t b = 0; b < plans[live[li]].cols; b++) t += acc[(size_t) (colbase[li] + b)];
+      sums[live[li]] = t;
+    }
+    float ms = 0;
+    PCG_CUDA(cudaEventElapsedTime(&ms, c.ev[0], c.ev[1]));
+    st.leaves = ctr[0];
+    st.two_prime_leaves = ctr[1];
+    st.levels = ctr[2];
+    st.factor_entries = ctr[3];
+    st.crossoff_multiples = ctr[4];
+    st.sweep_ms = ms;
+    st.sweep_kernel_ms = ms;
+    st.sweep_launches = waves.size();
+    st.kernel_launches = 2 * waves.size();
+    st.segments = (uint64_t) nitems;
+    st.h2d_bytes = seg_all.size() * 8 + xp_all.size() * 8 + qs.size() * sizeof(SweepQ) + rows.size() * 8 +
+                   jobs.size() * sizeof(CombineJob);
+    st.d2h_bytes = (uint64_t) ncells * 16 + sizeof(ctr);
+    st.segment_words = words;
+    st.ctas_per_sm = ctas;
+    st.threads_per_cta = NT;
+  } catch (...) {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    throw;
+  }
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(graph);
+  st.total_ms = now_ms() - t_start;
+  if (stp) *stp = st;
+}
+
 // ================================================================ allocation-free D
 // Some callers cannot allocate device memory at the time they need D(x): a
 // serving loop that must not touch the allocator on its request path, or a
@@ -2152,6 +2591,7 @@ SweepResult run_sweep(Ctx& c, const SweepProblem& pb, const Tuning& tune_in, cud
 #define PCG_NOALLOC_SCRATCH_BYTES (64ull << 20)
 #define PCG_NOALLOC_MAX_COLS 32768
 #define PCG_NOALLOC_MAX_SEGS (1 << 20)
+#define PCG_NOALLOC_MAX_ROWS (1 << 16)
 static __device__ __align__(256) unsigned char g_noalloc_scratch[PCG_NOALLOC_SCRATCH_BYTES];
 
 // Device address of the scratch array for device dev.  Host code only holds
@@ -2186,6 +2626,9 @@ SweepResult run_sweep_noalloc(Ctx& c, const SweepProblem& pb, cudaStream_t s)
   static int64_t h_nseg = -1;
   static int64_t h_plan_key[8];
   static i128 h_acc[PCG_NOALLOC_MAX_COLS];
+  static SweepQ h_q;
+  static int64_t h_row[PCG_NOALLOC_MAX_ROWS];
+  static CombineJob h_jobs[2 * (PCG_NOALLOC_MAX_COLS / 32 + 2)];
   std::lock_guard<std::mutex> guard(call_mu);
   SweepResult res;
   pcg_stats& st = res.stats;
@@ -2273,8 +2716,18 @@ SweepResult run_sweep_noalloc(Ctx& c, const SweepProblem& pb, cudaStream_t s)
   if (fixed + per_row > PCG_NOALLOC_SCRATCH_BYTES)
     fail(PCG_ERANGE, "pcg_D_noalloc: needs more than the " + std::to_string(PCG_NOALLOC_SCRATCH_BYTES) +
                          "-byte static scratch (x too large for the allocation-free path)");
-  int64_t wave_len = std::min<int64_t>({nseg, (int64_t) grid * 8,
-                                        (int64_t) ((PCG_NOALLOC_SCRATCH_BYTES - fixed) / per_row)});
+  const int njobs = (cols + 31) / 32 + 1;
+  const size_t jobs_bytes = (size_t) 2 * njobs * sizeof(CombineJob);
+  int64_t wave_len = std::min<int64_t>({nseg, (int64_t) grid * 8, (int64_t) PCG_NOALLOC_MAX_ROWS,
+                                        (int64_t) ((PCG_NOALLOC_SCRATCH_BYTES - fixed - align(jobs_bytes) - 512) /
+                                                   (per_row + 8))});
+  if (wave_len < 1) fail(PCG_ERANGE, "pcg_D_noalloc: x too large for the allocation-free path");
+  SweepQ* d_q = (SweepQ*) (scratch + off);
+  off = align(off + sizeof(SweepQ));
+  CombineJob* d_jobs = (CombineJob*) (scratch + off);
+  off = align(off + jobs_bytes);
+  int64_t* d_row = (int64_t*) (scratch + off);
+  off = align(off + (size_t) wave_len * 8);
   int64_t* d_segsum = (int64_t*) (scratch + off);
   off = align(off + (size_t) wave_len * 8);
   uint32_t* d_cnt = (uint32_t*) (scratch + off);
@@ -2283,27 +2736,41 @@ SweepResult run_sweep_noalloc(Ctx& c, const SweepProblem& pb, cudaStream_t s)
   off = align(off + (size_t) wave_len * cols * 4);
   if (off > PCG_NOALLOC_SCRATCH_BYTES) fail(PCG_EINTERNAL, "no-alloc scratch carve overflow");
 
+  memset(&h_q, 0, sizeof(h_q));
+  h_q.x_lo = (uint64_t) x;
+  h_q.x_hi = (uint64_t) (x >> 64);
+  h_q.y = pb.y;
+  h_q.z = pb.z;
+  h_q.k = pb.k;
+  h_q.L = L;
+  h_q.x_star = x_star;
+  h_q.item0 = 0;
+  h_q.seglo = d_seg;
+  h_q.xp_tab = d_xp;
+  h_q.gourdon = 1;
+  h_q.pi_sqrt = (int) pi_sqrt;
+  h_q.bglob = (int) bglob;
+  for (int64_t i = 0; i < wave_len; i++) h_row[i] = i * cols;
+  const int64_t last_len = (nseg - 1) % wave_len + 1;
+  for (int pass = 0; pass < 2; pass++) {
+    const int n = (int) (pass == 0 ? wave_len : last_len);
+    CombineJob* J = h_jobs + pass * njobs;
+    for (int sl = 0; sl * 32 < cols; sl++) J[sl] = CombineJob{0, 0, n, cols, sl};
+    J[njobs - 1] = CombineJob{0, 0, n, cols, -1};
+  }
+
   SweepArgs a;
   memset(&a, 0, sizeof(a));
-  a.x_lo = (uint64_t) x;
-  a.x_hi = (uint64_t) (x >> 64);
-  a.y = pb.y;
-  a.z = pb.z;
-  a.k = pb.k;
-  a.L = L;
-  a.x_star = x_star;
-  a.seglo = d_seg;
+  a.qs = d_q;
+  a.nq = 1;
+  a.rowoff = d_row;
   a.words = words;
   a.rec_cap = cap;
-  a.gourdon = 1;
-  a.pi_sqrt = (int) pi_sqrt;
-  a.bglob = (int) bglob;
   a.primes = T.primes.as<uint32_t>();
   a.nprimes = T.nprimes;
   a.pitab = T.pitab.as<uint64_t>();
   a.pi_max = T.prime_limit;
   a.factor = T.factor_d.p;
-  a.xp_tab = d_xp;
   a.coprime = T.coprime.as<uint16_t>();
   a.group_max = sweep_group_max();
   a.cindex = T.cindex.as<int16_t>();
@@ -2323,6 +2790,9 @@ SweepResult run_sweep_noalloc(Ctx& c, const SweepProblem& pb, cudaStream_t s)
     PCG_CUDA(cudaMemsetAsync(d_acc, 0, (size_t) cols * 16, s));
     PCG_CUDA(cudaMemcpyAsync(d_xp, h_xp, (size_t) cols * 24, cudaMemcpyHostToDevice, s));
     PCG_CUDA(cudaMemcpyAsync(d_seg, h_seg, (size_t) (nseg + 1) * 8, cudaMemcpyHostToDevice, s));
+    PCG_CUDA(cudaMemcpyAsync(d_q, &h_q, sizeof(SweepQ), cudaMemcpyHostToDevice, s));
+    PCG_CUDA(cudaMemcpyAsync(d_row, h_row, (size_t) wave_len * 8, cudaMemcpyHostToDevice, s));
+    PCG_CUDA(cudaMemcpyAsync(d_jobs, h_jobs, jobs_bytes, cudaMemcpyHostToDevice, s));
     for (int64_t first = 0; first < nseg; first += wave_len) {
       int wl = (int) std::min<int64_t>(wave_len, nseg - first);
       a.wave_first = first;
@@ -2335,10 +2805,10 @@ SweepResult run_sweep_noalloc(Ctx& c, const SweepProblem& pb, cudaStream_t s)
       if (fbytes == 2) launch_sweep<uint16_t, 256>(a, g, smem, s);
       else launch_sweep<uint32_t, 256>(a, g, smem, s);
       PCG_CUDA(cudaGetLastError());
-      k_combine<<<(cols + 31) / 32, 32 * COMBINE_WARPS, 0, s>>>(d_cnt, d_smu, wl, cols, d_run, d_acc, nullptr);
-      k_segsum<<<1, 1024, 0, s>>>(d_segsum, wl, d_acc);
+      k_combine<<<njobs, 32 * COMBINE_WARPS, 0, s>>>(d_cnt, d_smu, d_row, d_segsum,
+                                                    d_jobs + (wl == wave_len ? 0 : njobs), d_run, d_acc, nullptr);
       PCG_CUDA(cudaGetLastError());
-      launches += 3;
+      launches += 2;
       waves++;
     }
     PCG_CUDA(cudaMemcpyAsync(h_acc, d_acc, (size_t) cols * 16, cudaMemcpyDeviceToHost, s));
@@ -2362,7 +2832,8 @@ SweepResult run_sweep_noalloc(Ctx& c, const SweepProblem& pb, cudaStream_t s)
   st.segments = (uint64_t) nseg;
   st.kernel_launches = launches;
   st.sweep_launches = (uint64_t) waves;
-  st.h2d_bytes = (uint64_t) cols * 24 + (uint64_t) (nseg + 1) * 8;
+  st.h2d_bytes = (uint64_t) cols * 24 + (uint64_t) (nseg + 1) * 8 + sizeof(SweepQ) + (uint64_t) wave_len * 8 +
+                 jobs_bytes;
   st.d2h_bytes = (uint64_t) cols * 16 + sizeof(ctr);
   st.segment_words = words;
   st.ctas_per_sm = ctas;

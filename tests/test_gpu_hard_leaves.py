@@ -34,19 +34,20 @@ def test_S2_hard_random_fixture(pcg, golden):
 
 
 def test_D_default_large(pcg, golden):
-    for xs, row in sorted(golden["D_default"].items(), key=lambda kv: int(kv[0])):
-        x = int(xs)
-        if x > 10 ** 20:
-            continue
-        assert pcg.D(x, row["y"], row["z"], row["k"]) == row["D"], xs
+    # D at 1e15 ... 1e22 from the reference binary; x >= 1e20 > 2^64 takes the
+    # int128 path (src/gourdon/D.cpp:456-505)
+    rows = sorted(golden["D_default"].items(), key=lambda kv: int(kv[0]))
+    assert int(rows[-1][0]) >= 10 ** 22
+    for xs, row in rows:
+        assert pcg.D(int(xs), row["y"], row["z"], row["k"]) == row["D"], xs
 
 
 def test_S2_hard_default_large(pcg, golden):
-    for xs, row in sorted(golden["S2_hard_default"].items(), key=lambda kv: int(kv[0])):
-        x = int(xs)
-        if x > 10 ** 19:
-            continue
-        assert pcg.S2_hard(x, row["y"], row["z"], row["c"]) == row["S2_hard"], xs
+    # S2_hard at 1e15 ... 1e20 from the reference binary
+    rows = sorted(golden["S2_hard_default"].items(), key=lambda kv: int(kv[0]))
+    assert int(rows[-1][0]) >= 10 ** 20
+    for xs, row in rows:
+        assert pcg.S2_hard(int(xs), row["y"], row["z"], row["c"]) == row["S2_hard"], xs
 
 
 def test_leaf_count_matches_oracle(pcg, ora):
