@@ -92,9 +92,51 @@ $(OUT)/primecount: $(APP_OBJ) $(OUT)/libprimecount_ref.a
 $(OUT)/build_flags.txt: $(OUT)/primecount
 	@echo "arch=$(ARCH) cxx=$$($(CXX) -dumpfullversion) flags=$(CXXFLAGS) defs=$(DEFS) primesieve_defs=$(PS_DEFS)" > $@
 
+# Integration check: the reference's own test programs for the hard leaves
+# (test/gourdon/D.cpp, test/deleglise-rivat/S2_hard_alpha.cpp,
+# test/gourdon/pi_gourdon.cpp), linked with the drop-in D() / S2_hard() of
+# primecount_gb300/integration/hard_leaves_gpu.cpp (which calls libpcgpu)
+# and with the reference's own bodies renamed D_cpu / S2_hard_cpu.
+#   make -f oracle/ref.mk REF=... itest PCGPU=<repository root>
+PCGPU  ?= .
+ITEST  := $(OUT)/itest
+ITEST_PROGS := $(ITEST)/test_D $(ITEST)/test_S2_hard_alpha $(ITEST)/test_pi_gourdon
+NOHARD_OBJ := $(filter-out %/gourdon/D.o %/deleglise-rivat/S2_hard.o,$(PC_OBJ)) $(PS_OBJ)
+
+itest: $(ITEST_PROGS)
+
+$(ITEST)/D_cpu.o: $(REF)/src/gourdon/D.cpp
+	@mkdir -p $(dir $@)
+	$(CXX) $(CXXFLAGS) $(DEFS) $(INC) -DD=D_cpu -c $< -o $@
+
+$(ITEST)/S2_hard_cpu.o: $(REF)/src/deleglise-rivat/S2_hard.cpp
+	@mkdir -p $(dir $@)
+	$(CXX) $(CXXFLAGS) $(DEFS) $(INC) -DS2_hard=S2_hard_cpu -c $< -o $@
+
+$(ITEST)/hard_leaves_gpu.o: $(PCGPU)/primecount_gb300/integration/hard_leaves_gpu.cpp
+	@mkdir -p $(dir $@)
+	$(CXX) $(CXXFLAGS) $(DEFS) $(INC) -I$(PCGPU)/include -c $< -o $@
+
+$(ITEST)/libref_nohard.a: $(NOHARD_OBJ)
+	@mkdir -p $(dir $@)
+	rm -f $@ && ar rcs $@ $^
+
+ITEST_LINK := $(ITEST)/hard_leaves_gpu.o $(ITEST)/D_cpu.o $(ITEST)/S2_hard_cpu.o $(ITEST)/libref_nohard.a \
+              -L$(abspath $(PCGPU))/primecount_gb300 -lpcgpu -Wl,-rpath,$(abspath $(PCGPU))/primecount_gb300
+
+$(ITEST)/test_D: $(REF)/test/gourdon/D.cpp $(ITEST)/hard_leaves_gpu.o $(ITEST)/D_cpu.o $(ITEST)/S2_hard_cpu.o $(ITEST)/libref_nohard.a
+	$(CXX) $(CXXFLAGS) $(DEFS) $(INC) $< $(ITEST_LINK) -o $@
+
+$(ITEST)/test_S2_hard_alpha: $(REF)/test/deleglise-rivat/S2_hard_alpha.cpp $(ITEST)/hard_leaves_gpu.o $(ITEST)/D_cpu.o $(ITEST)/S2_hard_cpu.o $(ITEST)/libref_nohard.a
+	$(CXX) $(CXXFLAGS) $(DEFS) $(INC) $< $(ITEST_LINK) -o $@
+
+$(ITEST)/test_pi_gourdon: $(REF)/test/gourdon/pi_gourdon.cpp $(ITEST)/hard_leaves_gpu.o $(ITEST)/D_cpu.o $(ITEST)/S2_hard_cpu.o $(ITEST)/libref_nohard.a
+	$(CXX) $(CXXFLAGS) $(DEFS) $(INC) $< $(ITEST_LINK) -o $@
+
 # the sources compiled above plus the headers they include
 stage:
 	@mkdir -p $(STAGE)
-	cd $(REF) && cp -r --parents include src lib/primesieve/include lib/primesieve/src COPYING $(abspath $(STAGE))/
+	cd $(REF) && cp -r --parents include src lib/primesieve/include lib/primesieve/src \
+	  test/gourdon/D.cpp test/deleglise-rivat/S2_hard_alpha.cpp test/gourdon/pi_gourdon.cpp COPYING $(abspath $(STAGE))/
 
-.PHONY: all stage
+.PHONY: all stage itest

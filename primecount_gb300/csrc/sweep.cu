@@ -1258,8 +1258,10 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
               // the number's 32-bit half-word, and the half-word stride
               uint32_t h = 2 * w + (bi >> 5);
               const uint32_t hstep = (uint32_t) p * (NT / 32);
+              uint32_t* const hw = (uint32_t*) bits;
               for (uint32_t j = tid; j < P.jn; j += NT, h += hstep) {
-                if (atomicAnd((uint32_t*) bits + h, ~m) & m) { rem++; atomicSub(&ccount[h >> 4], 1u); }
+                const uint32_t old = hw[h];
+                if (old & m) { hw[h] = old & ~m; rem++; atomicSub(&ccount[h >> 4], 1u); }
               }
             }
           }

@@ -81,8 +81,9 @@ def main():
 
     todo = [("pi", i) for i in range(a.n) if data["pi"][i] is None]
     todo += [("phi", i) for i in range(a.n) if data["phi"][i] is None]
-    # largest first, so that the pool ends on small queries
-    todo.sort(key=lambda t: -(xs[t[1]] if t[0] == "pi" else px[t[1]] ** 1.15))
+    # the pi queries first, each kind largest first, so that the pool ends on
+    # small queries
+    todo.sort(key=lambda t: (t[0] != "pi", -(xs[t[1]] if t[0] == "pi" else px[t[1]])))
     done = 0
     with cf.ThreadPoolExecutor(max_workers=a.jobs) as ex:
         for _ in cf.as_completed([ex.submit(job, k, i) for k, i in todo]):
