@@ -107,34 +107,33 @@ def measured_peaks():
 
 
 def profile_traffic():
-    """DRAM bytes per algorithmic byte of k_sweep, from the committed summary
-    of an ncu capture of every k_sweep launch of a smaller D (its line
-    `dram_bytes_per_alg_byte: R`), if present; scaled to a launch of this
-    workload by its algorithmic bytes."""
-    p = os.path.join(ROOT, "profiles", "k_sweep_traffic_D1e18.md")
+    """DRAM bytes per k_sweep launch of D(1e20), from the committed summary of
+    an ncu capture of every k_sweep launch of one D(1e20) (its line
+    `dram_bytes_per_launch: N`), if present."""
+    p = os.path.join(ROOT, "profiles", "k_sweep_traffic_D1e20.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
-        if line.strip().startswith("dram_bytes_per_alg_byte:"):
+        if line.strip().startswith("dram_bytes_per_launch:"):
             try:
-                return {"ratio": float(line.split(":", 1)[1].strip().split()[0]),
-                        "source": "profiles/k_sweep_traffic_D1e18.md"}
+                return {"bytes": float(line.split(":", 1)[1].strip().split()[0]),
+                        "source": "profiles/k_sweep_traffic_D1e20.md"}
             except ValueError:
                 return None
     return None
 
 
 def profile_issue():
-    """Issue-slot use of k_sweep (ncu smsp__issue_active, % of peak) in a sparse
-    and a dense wave of D(1e19), from the committed capture summary: the
-    kernel is bound by the per-level chain and integer issue, not by HBM."""
-    p = os.path.join(ROOT, "profiles", "k_sweep_D1e19.md")
+    """Issue-slot use of k_sweep (ncu smsp__issue_active, % of peak) in a dense
+    and a sparse wave of D(1e18), from the committed capture summary: the
+    kernel is bound by integer issue and the per-level chain, not by HBM."""
+    p = os.path.join(ROOT, "profiles", "k_sweep_D1e18.md")
     try:
         for line in open(p):
             if "smsp__issue_active" in line:
                 cells = [c.strip() for c in line.strip().strip("|").split("|")]
-                return {"sparse_wave_pct": float(cells[1].split()[0]), "dense_wave_pct": float(cells[2].split()[0]),
-                        "source": "profiles/k_sweep_D1e19.md"}
+                return {"dense_wave_pct": float(cells[1].split()[0]), "sparse_wave_pct": float(cells[2].split()[0]),
+                        "source": "profiles/k_sweep_D1e18.md"}
     except (OSError, ValueError, IndexError):
         return None
     return None
@@ -213,16 +212,20 @@ def batch_workload(n, pcg):
     with the reference's answers, from the committed fixture
     (tests/golden/gen_batch.py); without it, the same generator and no
     reference answers."""
+    import math
     if os.path.exists(BATCH_FIXTURE):
         d = json.load(open(BATCH_FIXTURE))
         if d.get("n", 0) >= n:
             xs = [int(v) for v in d["pi_x"][:n]]
             px = [int(v) for v in d["phi_x"][:n]]
+            us = d["phi_u"][:n]
             pa = d["phi_a"][:n]
-            if all(a is not None for a in pa):
-                return (xs, [None if v is None else int(v) for v in d["pi"][:n]], px, [int(a) for a in pa],
-                        [None if v is None else int(v) for v in d["phi"][:n]], "tests/golden/batch_4096.json")
-    import math
+            if any(a is None for a in pa):
+                # a = 1 + floor(u pi(floor(sqrt x))) where the fixture has no answer yet
+                pis = pcg.pi_batch([math.isqrt(x) for x in px])
+                pa = [a if a is not None else 1 + int(u * max(1, p)) for a, u, p in zip(pa, us, pis)]
+            return (xs, [None if v is None else int(v) for v in d["pi"][:n]], px, [int(a) for a in pa],
+                    [None if v is None else int(v) for v in d["phi"][:n]], "tests/golden/batch_4096.json")
     sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
     import gen_batch
     xs, px, us = gen_batch.inputs(n)
@@ -245,22 +248,36 @@ def run_batch(args, pcg):
     bad = sum(1 for g, w in checked if g != w)
     if bad:
         raise SystemExit("batch: %d answers differ from the reference fixture" % bad)
-    m = min(args.plain_sample, n)
-    # plain: one query per call, tables built inside (fresh context), on an
-    # evenly spread sample of the same queries
-    idx = [(i * n) // m for i in range(m)]
-    tp = []
-    for i in idx:
-        for kind in ("pi", "phi"):
-            c = pcg.Context(0)
-            a0 = time.perf_counter()
-            v = pcg.pi(xs[i], ctx=c) if kind == "pi" else pcg.phi(px[i], pa[i], ctx=c)
-            tp.append((kind, time.perf_counter() - a0))
-            c.close()
-            if v != (r_pi[i] if kind == "pi" else r_phi[i]):
-                raise SystemExit("batch: the plain answer differs from the batched one (%s, %d)" % (kind, i))
-    plain_pi = sorted(t for k, t in tp if k == "pi")
-    plain_phi = sorted(t for k, t in tp if k == "phi")
+    # plain: one query per call, tables built inside (fresh context), on a
+    # sample stratified by decade of x (the time of a query grows steeply
+    # with x, so an unstratified sample of a few dozen queries misses the
+    # largest ones): per decade the mean time of its sampled queries times
+    # its number of queries estimates the whole batch's plain time
+    import math
+    per = max(1, args.plain_sample // 8)
+
+    def plain(kind, xs_, fn, want):
+        dec = {}
+        for i, x in enumerate(xs_):
+            dec.setdefault(int(math.log10(max(x, 1))), []).append(i)
+        est, times = 0.0, []
+        for d, idx in sorted(dec.items()):
+            pick = [idx[(j * len(idx)) // per] for j in range(min(per, len(idx)))]
+            ts = []
+            for i in pick:
+                c = pcg.Context(0)
+                a0 = time.perf_counter()
+                v = fn(i, c)
+                ts.append(time.perf_counter() - a0)
+                c.close()
+                if v != want[i]:
+                    raise SystemExit("batch: the plain answer differs from the batched one (%s, %d)" % (kind, i))
+            times += ts
+            est += len(idx) * sum(ts) / len(ts)
+        return est, sorted(times)
+
+    est_pi, plain_pi = plain("pi", xs, lambda i, c: pcg.pi(xs[i], ctx=c), r_pi)
+    est_phi, plain_phi = plain("phi", px, lambda i, c: pcg.phi(px[i], pa[i], ctx=c), r_phi)
 
     def p99(v):
         return v[min(len(v) - 1, int(round(0.99 * (len(v) - 1))))] if v else None
@@ -269,10 +286,13 @@ def run_batch(args, pcg):
                        "seconds": t2 - t0, "pi_seconds": t1 - t0, "phi_seconds": t2 - t1,
                        "latency_note": "one call per kind: every query of a call completes when the call returns "
                                        "(p99 latency = the call's wall time)"},
-            "plain_sample": {"queries_per_kind": m, "pi_qps": len(plain_pi) / max(sum(plain_pi), 1e-9),
-                             "phi_qps": len(plain_phi) / max(sum(plain_phi), 1e-9),
-                             "pi_p99_s": p99(plain_pi), "phi_p99_s": p99(plain_phi),
-                             "note": "evenly spread queries of the same batch, one per call, fresh context"},
+            "plain_sample": {"queries_per_kind": len(plain_pi), "per_decade": per,
+                             "pi_qps": n / est_pi, "phi_qps": n / est_phi,
+                             "pi_seconds_est": est_pi, "phi_seconds_est": est_phi,
+                             "all_qps": 2 * n / (est_pi + est_phi),
+                             "pi_p99_of_sample_s": p99(plain_pi), "phi_p99_of_sample_s": p99(plain_phi),
+                             "note": "the same batch one query per call (fresh context): per decade of x the mean "
+                                     "time of an evenly spread sample times the decade's number of queries"},
             "checks": {"reference_answers_checked": len(checked), "mismatches": bad,
                        "plain_equal_batched": True}}
 
@@ -510,7 +530,7 @@ def main():
     launch_s = k_ms_call / launches_call / 1000.0
     achieved = alg_bytes / launches_call / launch_s / 1e9
     tr = profile_traffic()
-    traffic = tr["ratio"] * alg_bytes / launches_call if tr else None
+    traffic = tr["bytes"] if tr and X == 10 ** 20 else None
     # algorithmic integer / shared-memory operations: per leaf one division
     # and one prefix query (a counter load and up to 8 popcounts), per
     # cross-off multiple one shared-memory read-modify-write; against the

@@ -444,6 +444,46 @@ __device__ __forceinline__ bool cross_off(uint64_t* bits, uint32_t w, uint32_t r
   return (atomicAnd((uint32_t*) bits + 2 * w + (bi >> 5), ~m) & m) != 0;
 }
 
+// Cross off the multiples of the levels [l0, l1) at once (their co-factor
+// counts prefixed in hoff): with few multiples per level a warp takes each
+// level and its lanes the level's multiples; otherwise the multiples are
+// spread flat over the threads, each finding its level by a binary search.
+// Different levels can share a half-word, so the clears are atomic.
+template <int NT>
+__device__ __forceinline__ void cross_off_levels(uint64_t* bits, uint32_t* ccount, const LevelP* lp,
+                                                 const int64_t* hoff, int l0, int l1, uint64_t low)
+{
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t h0 = hoff[l0], h1 = hoff[l1];
+  if (h1 - h0 <= 64 * (int64_t) (l1 - l0)) {
+    for (int lv = l0 + warp; lv < l1; lv += NT / 32) {
+      const uint64_t prime = lp[lv].prime, jlo = lp[lv].jlo;
+      const uint32_t jn = (uint32_t) (hoff[lv + 1] - hoff[lv]);
+      for (uint32_t j = lane; j < jn; j += 32) {
+        const uint64_t jj = jlo + j;
+        const uint64_t q = 30 * (jj >> 3) + woff((uint32_t) (jj & 7));
+        const uint32_t off = (uint32_t) (prime * q - low);
+        const uint32_t w = off / 240, rr = off - w * 240;
+        if (cross_off(bits, w, rr)) atomicSub(&ccount[w >> 3], 1u);
+      }
+    }
+    return;
+  }
+  for (int64_t h = h0 + tid; h < h1; h += NT) {
+    int lo = l0, hi = l1 - 1;       // last level with hoff <= h
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (hoff[mid] <= h) lo = mid; else hi = mid - 1;
+    }
+    const LevelP& Q = lp[lo];
+    const uint64_t jj = Q.jlo + (uint64_t) (h - hoff[lo]);
+    const uint64_t q = 30 * (jj >> 3) + woff((uint32_t) (jj & 7));
+    const uint32_t off = (uint32_t) ((uint64_t) Q.prime * q - low);
+    const uint32_t w = off / 240, rr = off - w * 240;
+    if (cross_off(bits, w, rr)) atomicSub(&ccount[w >> 3], 1u);
+  }
+}
+
 // Record of one table entry: the offset of the leaf in the segment, bit 30 =
 // negative sign, or REC_NONE when the factor-table filter rejects the entry.
 #define REC_NONE 0xFFFFFFFFu
@@ -1012,19 +1052,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
             for (int t = tid; t < re - li; t += NT)
               A.cnt[rowbase + b0 + li + t] = total - (uint32_t) (rpre[li + t] - r0);
             const int64_t h0 = hoff[li], h1 = hoff[re];
-            for (int64_t h = h0 + tid; h < h1; h += NT) {
-              int lo = li, hi = re - 1;       // last level with hoff <= h
-              while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (hoff[mid] <= h) lo = mid; else hi = mid - 1;
-              }
-              const LevelP& Q = lp[lo];
-              const uint64_t jj = Q.jlo + (uint64_t) (h - hoff[lo]);
-              const uint64_t q = 30 * (jj >> 3) + woff((uint32_t) (jj & 7));
-              const uint32_t off = (uint32_t) ((uint64_t) Q.prime * q - (uint64_t) low);
-              const uint32_t w = off / 240, rr = off - w * 240;
-              if (cross_off(bits, w, rr)) atomicSub(&ccount[w >> 3], 1u);
-            }
+            cross_off_levels<NT>(bits, ccount, lp, hoff, li, re, (uint64_t) low);
             const uint32_t removed = (uint32_t) (rpre[re] - r0);
             total -= removed;
             if (h1 > h0) dirty = true;
@@ -1145,19 +1173,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
               }
               // all their multiples crossed off at once
               const int64_t h0 = hoff[li], h1 = hoff[lj];
-              for (int64_t h = h0 + tid; h < h1; h += NT) {
-                int lo = li, hi = lj - 1;       // last level with hoff <= h
-                while (lo < hi) {
-                  const int mid = (lo + hi + 1) >> 1;
-                  if (hoff[mid] <= h) lo = mid; else hi = mid - 1;
-                }
-                const LevelP& Q = lp[lo];
-                const uint64_t jj = Q.jlo + (uint64_t) (h - hoff[lo]);
-                const uint64_t q = 30 * (jj >> 3) + woff((uint32_t) (jj & 7));
-                const uint32_t off = (uint32_t) ((uint64_t) Q.prime * q - (uint64_t) low);
-                const uint32_t w = off / 240, rr = off - w * 240;
-                if (cross_off(bits, w, rr)) atomicSub(&ccount[w >> 3], 1u);
-              }
+              cross_off_levels<NT>(bits, ccount, lp, hoff, li, lj, (uint64_t) low);
               total -= (uint32_t) (rpre[lj] - r0);
               if (h1 > h0) dirty = true;
               li = lj;
@@ -1226,21 +1242,27 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
             const uint32_t p = P.prime;
             int po = 0;
             for (int k = 0; c_small_p[k] != p; k++) po += c_small_p[k];
-            uint32_t r = (uint32_t) ((P.jlo + tid) % p);
-            const uint32_t step = NT % p;
-            for (int w = tid; w < A.words; w += NT) {
+            // two consecutive words per thread and round (16-byte accesses)
+            uint32_t r = (uint32_t) ((P.jlo + 2 * tid) % p);
+            const uint32_t step = (2 * NT) % p;
+            for (int w = 2 * tid; w < A.words; w += 2 * NT) {
               uint32_t d = 0;
               if (w < wused) {
-                const uint64_t old = bits[w];
-                const uint64_t nw = old & pat[po + r];
-                if (nw != old) { bits[w] = nw; d = __popcll(old ^ nw); }
+                const ulonglong2 old = *(const ulonglong2*) (bits + w);
+                const uint32_t r1 = r + 1 == p ? 0u : r + 1;
+                ulonglong2 nw;
+                nw.x = old.x & pat[po + r];
+                nw.y = (w + 1 < wused) ? (old.y & pat[po + r1]) : old.y;
+                if (nw.x != old.x || nw.y != old.y) {
+                  *(ulonglong2*) (bits + w) = nw;
+                  d = __popcll(old.x ^ nw.x) + __popcll(old.y ^ nw.y);
+                }
               }
               rem += d;
-              // 8 consecutive lanes own the 8 words of one chunk
-              d += __shfl_down_sync(0xffffffffu, d, 4, 8);
-              d += __shfl_down_sync(0xffffffffu, d, 2, 8);
-              d += __shfl_down_sync(0xffffffffu, d, 1, 8);
-              if ((lane & 7) == 0 && d) ccount[w >> 3] -= d;
+              // 4 consecutive lanes own the 8 words of one chunk
+              d += __shfl_down_sync(0xffffffffu, d, 2, 4);
+              d += __shfl_down_sync(0xffffffffu, d, 1, 4);
+              if ((lane & 3) == 0 && d) ccount[w >> 3] -= d;
               r += step;
               if (r >= p) r -= p;
             }

@@ -17,6 +17,23 @@ def test_pi_batch_matches_fixture_and_single(pcg, golden):
     assert got[len(rows):] == alone
 
 
+def test_seeded_batch_against_the_reference(pcg):
+    """Config 4's seeded batch (tests/golden/batch_4096.json, answers from the
+    reference binary): every 8th query of each kind through the batch forms."""
+    import json
+    import os
+    p = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "batch_4096.json")
+    d = json.load(open(p))
+    idx = [i for i in range(0, d["n"], 8) if d["pi"][i] is not None]
+    assert len(idx) >= 256
+    got = pcg.pi_batch([int(d["pi_x"][i]) for i in idx])
+    assert got == [int(d["pi"][i]) for i in idx]
+    idx = [i for i in range(0, d["n"], 8) if d["phi"][i] is not None]
+    if idx:
+        got = pcg.phi_batch([int(d["phi_x"][i]) for i in idx], [d["phi_a"][i] for i in idx])
+        assert got == [int(d["phi"][i]) for i in idx]
+
+
 def test_phi_batch_matches_fixture(pcg, golden):
     rows = golden["phi_random"]
     got = pcg.phi_batch([r[0] for r in rows], [r[1] for r in rows])
