@@ -359,6 +359,17 @@ struct SweepArgs {
 #define PAT_WORDS 491   // 7+11+13+17+19+23+29+31+37+41+43+47+53+59+61
 __constant__ uint32_t c_small_p[NSMALL + 1] = {7, 11, 13, 17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61, 0};
 
+// min(floor(a / d), cap) for d >= 1, cap >= 0, with md = floor((2^64 - 1) / d):
+// one high product when a < 2^64
+__device__ __forceinline__ int64_t divcap_m(u128 a, uint64_t d, uint64_t md, int64_t cap)
+{
+  if ((uint64_t) (a >> 64) == 0) {
+    const uint64_t q = div_magic((uint64_t) a, d, md);
+    return q < (uint64_t) cap ? (int64_t) q : cap;
+  }
+  return divcap(a, d, cap);
+}
+
 // x / m for m < 2^32 when the quotient is known to fit in 63 bits
 __device__ __forceinline__ uint64_t div_xp32(uint64_t xlo, uint64_t xhi, uint32_t m)
 {
@@ -432,6 +443,28 @@ __device__ __forceinline__ uint32_t query(const uint64_t* __restrict__ bits, con
   };
   return pref[c] + part(0, w01.x) + part(1, w01.y) + part(2, w23.x) + part(3, w23.y) + part(4, w45.x) +
          part(5, w45.y) + part(6, w67.x) + part(7, w67.y);
+}
+
+// This lane's part of the sum of the chunk counts [0, ch): the lane takes the
+// 4-chunk groups lane, lane + 32, ... (16-byte loads, ch <= the number of
+// chunks, a multiple of 4), four groups' loads in flight together
+__device__ __forceinline__ uint32_t chunk_sum_below(const uint32_t* __restrict__ ccount, uint32_t ch, int lane)
+{
+  uint32_t part = 0;
+  for (uint32_t i0 = 0; i0 < ch; i0 += 512) {
+    uint4 v[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const uint32_t i = i0 + 128 * u + 4 * lane;
+      v[u] = i < ch ? *(const uint4*) (ccount + i) : make_uint4(0u, 0u, 0u, 0u);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const uint32_t i = i0 + 128 * u + 4 * lane;
+      part += v[u].x + (i + 1 < ch ? v[u].y : 0u) + (i + 2 < ch ? v[u].z : 0u) + (i + 3 < ch ? v[u].w : 0u);
+    }
+  }
+  return part;
 }
 
 // Cross off the number at offset w * 240 + rr of the segment: a 32-bit atomic
@@ -545,6 +578,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
   __shared__ int s_stop;
   __shared__ uint32_t s_rem[3];
   __shared__ uint32_t s_total;
+  __shared__ uint64_t s_mlow, s_mhigh;                 // floor((2^64 - 1) / d) of low1 and high
   __shared__ long long wt3[32][3];
   __shared__ int s_brk[32];
   __shared__ long long s_red[NT / 32];
@@ -627,6 +661,8 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
     }
     if (tid == 0) {
       s_total = 0; s_rem[0] = s_rem[1] = s_rem[2] = 0; s_smu = 0; s_stop = 0x7FFFFFFF;
+      s_mlow = UINT64_MAX / (uint64_t) low1;
+      s_mhigh = UINT64_MAX / (uint64_t) high;
       s_ncomp[0] = s_ncomp[1] = 0;
     }
     __syncthreads();
@@ -660,11 +696,12 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
         uint32_t ncross = 0;   // multiples of p_b in the segment (work counter)
         if (b <= Bs) {
           const uint64_t p = A.primes[b];
+          const uint64_t pm = A.pmagic[b];     // floor((2^64 - 1) / p): the divisions by p below
           P.prime = (uint32_t) p;
           if (p >= 64) {
-            uint64_t qlo = ((uint64_t) low + p - 1) / p;
+            uint64_t qlo = div_magic((uint64_t) low + p - 1, p, pm);
             if (qlo < 1) qlo = 1;
-            uint64_t qhi = ((uint64_t) high - 1) / p;
+            uint64_t qhi = div_magic((uint64_t) high - 1, p, pm);
             if (qlo <= qhi) {
               P.jlo = cnt_le(qlo - 1);
               P.jn = (uint32_t) (cnt_le(qhi) - P.jlo);
@@ -701,20 +738,20 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
               int64_t min_m, max_m;
               if (PQ.gourdon == 2) {
                 // phi(x, a): m in (max(y / p, x / (p high)), min(y, x / (p low))]
-                int64_t xp_high = divcap(xp, (uint64_t) high, PQ.y);
-                min_m = dmax(xp_high, PQ.y / prime);
-                max_m = divcap(xp, (uint64_t) low1, PQ.y);
+                int64_t xp_high = divcap_m(xp, (uint64_t) high, s_mhigh, PQ.y);
+                min_m = dmax(xp_high, (int64_t) div_magic((uint64_t) PQ.y, p, pm));
+                max_m = divcap_m(xp, (uint64_t) low1, s_mlow, PQ.y);
                 P.thr = (uint32_t) (2 * b + 1);
               } else if (PQ.gourdon) {
-                int64_t xp_low = divcap(xp, (uint64_t) low1, PQ.z);
-                int64_t xp_high = divcap(xp, (uint64_t) high, PQ.z);
-                min_m = dmax(xp_high, PQ.z / prime);
+                int64_t xp_low = divcap_m(xp, (uint64_t) low1, s_mlow, PQ.z);
+                int64_t xp_high = divcap_m(xp, (uint64_t) high, s_mhigh, PQ.z);
+                min_m = dmax(xp_high, (int64_t) div_magic((uint64_t) PQ.z, p, pm));
                 max_m = dmin(xpp, xp_low);
                 P.thr = (uint32_t) (2 * b + 1);
               } else {
-                int64_t xp_high = divcap(xp, (uint64_t) high, PQ.y);
-                min_m = dmax(xp_high, PQ.y / prime);
-                max_m = divcap(xp, (uint64_t) low1, PQ.y);
+                int64_t xp_high = divcap_m(xp, (uint64_t) high, s_mhigh, PQ.y);
+                min_m = dmax(xp_high, (int64_t) div_magic((uint64_t) PQ.y, p, pm));
+                max_m = divcap_m(xp, (uint64_t) low1, s_mlow, PQ.y);
                 P.thr = (uint32_t) prime;
               }
               if (prime >= max_m) stop = true;
@@ -724,15 +761,15 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                 if (P.hi > P.lo) P.flags |= 1;
               }
             } else {
-              int64_t xp_low = divcap(xp, (uint64_t) low1, PQ.y);
-              int64_t xp_high = divcap(xp, (uint64_t) high, PQ.y);
+              int64_t xp_low = divcap_m(xp, (uint64_t) low1, s_mlow, PQ.y);
+              int64_t xp_high = divcap_m(xp, (uint64_t) high, s_mhigh, PQ.y);
               int64_t l, min_hard;
               if (PQ.gourdon) {
                 int64_t max_m = dmin(xpp, xp_low);
                 l = dpi(A.pitab, (uint64_t) max_m);
                 min_hard = dmax(xp_high, prime);
               } else {
-                l = dpi(A.pitab, (uint64_t) dmin(xp_low, PQ.z / prime));
+                l = dpi(A.pitab, (uint64_t) dmin(xp_low, (int64_t) div_magic((uint64_t) PQ.z, p, pm)));
                 min_hard = dmax(xp_high, prime);
               }
               if (prime >= (int64_t) A.primes[l]) stop = true;
@@ -1091,11 +1128,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                   const uint32_t off = r & 0x3FFFFFFFu;
                   const uint64_t n = (uint64_t) low + off;
                   const uint32_t wd = off / 240, ch = wd >> 3, kw = wd & 7;
-                  uint32_t part = 0;
-                  for (uint32_t i = 4 * lane; i < ch; i += 128) {
-                    const uint4 v = *(const uint4*) (ccount + i);
-                    part += v.x + (i + 1 < ch ? v.y : 0u) + (i + 2 < ch ? v.z : 0u) + (i + 3 < ch ? v.w : 0u);
-                  }
+                  uint32_t part = chunk_sum_below(ccount, ch, lane);
                   if (lane < 8) {
                     const uint64_t v = bits[8 * ch + lane];
                     const uint32_t j = (uint32_t) lane;
@@ -1199,11 +1232,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                 if (r == REC_NONE) continue;
                 const uint32_t off = r & 0x3FFFFFFFu;
                 const uint32_t wd = off / 240, ch = wd >> 3, kw = wd & 7;
-                uint32_t part = 0;
-                for (uint32_t i = 4 * lane; i < ch; i += 128) {
-                  const uint4 v = *(const uint4*) (ccount + i);
-                  part += v.x + (i + 1 < ch ? v.y : 0u) + (i + 2 < ch ? v.z : 0u) + (i + 3 < ch ? v.w : 0u);
-                }
+                uint32_t part = chunk_sum_below(ccount, ch, lane);
                 if (lane < 8) {
                   const uint64_t v = bits[8 * ch + lane];
                   const uint32_t j = (uint32_t) lane;
