@@ -160,10 +160,12 @@ __global__ void __launch_bounds__(256) k_phi0(uint64_t x_lo, uint64_t x_hi, cons
 // ---------------------------------------------------------------- A and C
 // One outer item: a prime p_b (or p_b q for the C1 products) and a range
 // (i_lo, i_hi] of prime indices q = primes[i]; the term of q is
-//   mode 0 (A):  w * pi(xp / q), w = 1 if q <= cap else 2   (AC.cpp:40-83)
+//   mode 0 (A):  w * pi(xp / q), w = 1 if q <= xp / y else 2 (AC.cpp:40-83);
+//                cap holds the index pi(xp / y)
 //   mode 1 (C):  pi(xp / q) - b + 2                         (AC.cpp:112-129, 186-300)
 //   mode 2 (C1 products): -(pi(xp / q) - b + 2)              (AC.cpp:131-177)
 //   mode 3 (P3 of phi):   pi(xp / q) - i + 1, i = index of q
+//   modes 5, 6: modes 1, 2 of an outer whose xp / q can fall below 6
 struct PairOuter {
   uint64_t xp_lo, xp_hi;
   uint64_t cap;
@@ -192,41 +194,94 @@ static __device__ __forceinline__ long long pi_pt(const ulonglong2* __restrict__
   return (long long) e.x + __popcll(e.y & s_mask[r]);
 }
 
-template <int MODE>
-__device__ __forceinline__ long long pair_term(const PairOuter& O, uint32_t i, uint32_t q, uint64_t m,
-                                              const ulonglong2* __restrict__ pt, const uint64_t* s_mask)
+// pi(n) for n < 2^36: the word index by a 32-bit division
+static __device__ __forceinline__ long long pi_pt36(const ulonglong2* __restrict__ pt, const uint64_t* s_mask,
+                                                    uint64_t n)
 {
-  uint64_t n;
-  if (O.xp_hi == 0) n = div_magic(O.xp_lo, q, m);
-  else n = (uint64_t) ((((u128) O.xp_hi << 64) | O.xp_lo) / q);
-  // A: n = x / (p q) >= q > 6; the C and P3 terms can reach n < 6
-  const long long pin = (MODE != 0 && n < 6) ? (long long) ((0x322100u >> (4 * n)) & 15u) : pi_pt(pt, s_mask, n);
-  if (MODE == 0) return (q <= O.cap) ? pin : 2 * pin;
-  if (MODE == 1) return pin - O.b + 2;
-  if (MODE == 2) return -(pin - O.b + 2);
-  return pin - (long long) i + 1;
+  const uint32_t w32 = (uint32_t) (n >> 4) / 15u;
+  const uint32_t r = (uint32_t) n - 240u * w32;
+  const ulonglong2 e = pt[w32];
+  return (long long) e.x + __popcll(e.y & s_mask[r]);
 }
 
-// the terms of one outer (prime indices < 2^32), 256 threads, four terms per
-// thread in flight
-template <int MODE>
-__device__ __forceinline__ long long pair_terms(const PairOuter& O, const uint32_t* __restrict__ primes,
-                                                const uint64_t* __restrict__ magic,
-                                                const ulonglong2* __restrict__ pt, const uint64_t* s_mask)
+// pi(xp / q) for the prime q = primes[i] with m = floor((2^64 - 1) / q), by
+// shape of the outer:
+//   SHAPE 0: xp < 2^64, q < 2^31 and n < 2^36 (tables below those bounds):
+//            t = floor(xp * m / 2^64) is n or n - 1, and xp - t q < 2 q < 2^32,
+//            so its low 32 bits decide the correction;
+//   SHAPE 1: xp < 2^64 (64-bit remainder);  SHAPE 2: xp >= 2^64.
+// LOWN: the outer can reach n < 6, where the PiTable's first word (which
+// counts 2, 3 and 5 in every n) does not hold
+template <int SHAPE, bool LOWN>
+__device__ __forceinline__ long long pair_pi(const PairOuter& O, uint32_t q, uint64_t m,
+                                            const ulonglong2* __restrict__ pt, const uint64_t* s_mask)
+{
+  uint64_t n;
+  if (SHAPE == 0) {
+    n = __umul64hi(O.xp_lo, m);
+    n += ((uint32_t) O.xp_lo - (uint32_t) n * q) >= q;
+  } else if (SHAPE == 1) {
+    n = div_magic(O.xp_lo, q, m);
+  } else {
+    n = (uint64_t) ((((u128) O.xp_hi << 64) | O.xp_lo) / q);
+  }
+  if (LOWN && n < 6) return (long long) ((0x322100u >> (4 * n)) & 15u);
+  return SHAPE == 0 ? pi_pt36(pt, s_mask, n) : pi_pt(pt, s_mask, n);
+}
+
+// sum of pi(xp / q) over this thread's prime indices i in (lo, hi], i = lo +
+// 1 + threadIdx.x + 256 t (indices < 2^32), four terms in flight
+template <int SHAPE, bool LOWN>
+__device__ __forceinline__ long long pi_sum(const PairOuter& O, uint32_t lo, uint32_t hi,
+                                            const uint32_t* __restrict__ primes, const uint64_t* __restrict__ magic,
+                                            const ulonglong2* __restrict__ pt, const uint64_t* s_mask)
 {
   long long s = 0;
-  const uint32_t hi = (uint32_t) O.i_hi;
-  uint32_t i = (uint32_t) (O.i_lo + 1) + threadIdx.x;
+  uint32_t i = lo + 1 + threadIdx.x;
   for (; i + 3 * 256 <= hi; i += 4 * 256) {
     uint32_t q[4];
     uint64_t m[4];
 #pragma unroll
     for (int u = 0; u < 4; u++) { q[u] = primes[i + 256 * u]; m[u] = magic[i + 256 * u]; }
 #pragma unroll
-    for (int u = 0; u < 4; u++) s += pair_term<MODE>(O, i + 256 * u, q[u], m[u], pt, s_mask);
+    for (int u = 0; u < 4; u++) s += pair_pi<SHAPE, LOWN>(O, q[u], m[u], pt, s_mask);
   }
-  for (; i <= hi; i += 256) s += pair_term<MODE>(O, i, primes[i], magic[i], pt, s_mask);
+  for (; i <= hi; i += 256) s += pair_pi<SHAPE, LOWN>(O, primes[i], magic[i], pt, s_mask);
   return s;
+}
+
+// the terms of one outer for this thread; the per-term constants come out of
+// the sums: with c terms of indices i_1..i_c,
+//   mode 0: sum over i <= icap of pi + 2 * sum over i > icap  (icap = pi(cap))
+//   mode 1: sum pi - c (b - 2);   mode 2: -(sum pi - c (b - 2));
+//   mode 3: sum pi - sum (i - 1)
+template <int MODE, int SHAPE, bool LOWN>
+__device__ __forceinline__ long long pair_terms(const PairOuter& O, const uint32_t* __restrict__ primes,
+                                                const uint64_t* __restrict__ magic,
+                                                const ulonglong2* __restrict__ pt, const uint64_t* s_mask)
+{
+  const uint32_t lo = (uint32_t) O.i_lo, hi = (uint32_t) O.i_hi;
+  if (MODE == 0) {
+    const uint32_t ic = (uint32_t) min((uint64_t) hi, max((uint64_t) lo, O.cap));
+    return pi_sum<SHAPE, false>(O, lo, ic, primes, magic, pt, s_mask) +
+           2 * pi_sum<SHAPE, false>(O, ic, hi, primes, magic, pt, s_mask);
+  }
+  const long long s = pi_sum<SHAPE, LOWN>(O, lo, hi, primes, magic, pt, s_mask);
+  const uint32_t first = lo + 1 + threadIdx.x;
+  const long long c = first <= hi ? (long long) ((hi - first) / 256 + 1) : 0;
+  if (MODE == 1) return s - c * ((long long) O.b - 2);
+  if (MODE == 2) return -(s - c * ((long long) O.b - 2));
+  return s - c * ((long long) first - 1) - 256ll * (c * (c - 1) / 2);
+}
+
+template <int MODE, bool SMALL, bool LOWN>
+__device__ __forceinline__ long long outer_terms(const PairOuter& O, const uint32_t* __restrict__ primes,
+                                                 const uint64_t* __restrict__ magic,
+                                                 const ulonglong2* __restrict__ pt, const uint64_t* s_mask)
+{
+  if (O.xp_hi != 0) return pair_terms<MODE, 2, LOWN>(O, primes, magic, pt, s_mask);
+  if (SMALL) return pair_terms<MODE, 0, LOWN>(O, primes, magic, pt, s_mask);
+  return pair_terms<MODE, 1, LOWN>(O, primes, magic, pt, s_mask);
 }
 
 // outers of more than PAIR_SPLIT terms are cut into pieces of PAIR_SPLIT so
@@ -255,6 +310,8 @@ __global__ void k_pair_split(const PairOuter* __restrict__ outs, int64_t n, cons
   }
 }
 
+// SMALL: every prime of the table is below 2^31 and the PiTable ends below 2^36
+template <bool SMALL>
 __global__ void __launch_bounds__(256) k_pairs(const PairOuter* __restrict__ outs, int64_t n_outer,
                                                const uint32_t* __restrict__ primes,
                                                const uint64_t* __restrict__ magic,
@@ -268,10 +325,12 @@ __global__ void __launch_bounds__(256) k_pairs(const PairOuter* __restrict__ out
   for (int64_t o = blockIdx.x; o < n_outer; o += gridDim.x) {
     const PairOuter O = outs[o];
     long long s;
-    if (O.mode == 0) s = pair_terms<0>(O, primes, magic, pt, s_mask);
-    else if (O.mode == 1) s = pair_terms<1>(O, primes, magic, pt, s_mask);
-    else if (O.mode == 2) s = pair_terms<2>(O, primes, magic, pt, s_mask);
-    else s = pair_terms<3>(O, primes, magic, pt, s_mask);
+    if (O.mode == 0) s = outer_terms<0, SMALL, false>(O, primes, magic, pt, s_mask);
+    else if (O.mode == 1) s = outer_terms<1, SMALL, false>(O, primes, magic, pt, s_mask);
+    else if (O.mode == 2) s = outer_terms<2, SMALL, false>(O, primes, magic, pt, s_mask);
+    else if (O.mode == 3) s = outer_terms<3, SMALL, false>(O, primes, magic, pt, s_mask);
+    else if (O.mode == 5) s = outer_terms<1, SMALL, true>(O, primes, magic, pt, s_mask);
+    else s = outer_terms<2, SMALL, true>(O, primes, magic, pt, s_mask);
     acc += s;
   }
   block_sum_i128<256>(acc, &partial[blockIdx.x]);
@@ -302,8 +361,13 @@ static i128 run_pairs(Ctx& c, const PairOuter* outs, int64_t nout, cudaStream_t 
   DevBuf& part = c.tmp[T_PR_PART];
   part.alloc((size_t) grid * 16);
   PCG_CUDA(cudaMemsetAsync(part.p, 0, (size_t) grid * 16, s));
-  k_pairs<<<grid, 256, 0, s>>>(split.as<PairOuter>(), (int64_t) np, c.tab.primes.as<uint32_t>(),
-                               c.tab.pmagic.as<uint64_t>(), c.tab.pibig.as<uint64_t>(), part.as<i128>());
+  const bool small = c.tab.prime_limit < (1ll << 31) && c.tab.pibig_limit + 240 < (1ll << 36);
+  if (small)
+    k_pairs<true><<<grid, 256, 0, s>>>(split.as<PairOuter>(), (int64_t) np, c.tab.primes.as<uint32_t>(),
+                                       c.tab.pmagic.as<uint64_t>(), c.tab.pibig.as<uint64_t>(), part.as<i128>());
+  else
+    k_pairs<false><<<grid, 256, 0, s>>>(split.as<PairOuter>(), (int64_t) np, c.tab.primes.as<uint32_t>(),
+                                        c.tab.pmagic.as<uint64_t>(), c.tab.pibig.as<uint64_t>(), part.as<i128>());
   PCG_CUDA(cudaGetLastError());
   if (launches) *launches += 6;
   return sum_partials(part, grid, s);
@@ -332,10 +396,11 @@ __global__ void k_outer_A(AcParams P, PairOuter* __restrict__ outs)
   PairOuter O;
   O.xp_lo = (uint64_t) xp;
   O.xp_hi = (uint64_t) (xp >> 64);
-  O.cap = (uint64_t) (xp / (u128) P.y);
   O.b = (int32_t) b;
   O.mode = 0;
   const int64_t sq = disqrt(xp);
+  // xp / y <= sqrt(xp) since xp <= x / x* <= y^2
+  O.cap = (uint64_t) dpi(P.pibig, (uint64_t) dmin(sq, (int64_t) (xp / (u128) P.y)));
   const int64_t lowq = (int64_t) (xp / (u128) P.sqrtx);
   O.i_hi = dpi(P.pibig, (uint64_t) sq);
   O.i_lo = dmax(b, dpi(P.pibig, (uint64_t) lowq));
@@ -374,6 +439,7 @@ __global__ void k_outer_C1(AcParams P, PairOuter* __restrict__ outs)
   if (min_m < max_m && min_m < top) {
     O.i_lo = dpi(P.pismall, (uint64_t) min_m);
     O.i_hi = dpi(P.pismall, (uint64_t) top);
+    if (O.i_hi > O.i_lo && xp / P.primes[O.i_hi] < 6) O.mode = 5;
   }
   outs[j] = O;
 }
@@ -426,6 +492,7 @@ __global__ void k_c1_expand(AcParams P, const int64_t* __restrict__ qlo, const i
     if (min_r < max_r) {
       O.i_lo = dpi(P.pismall, (uint64_t) min_r);
       O.i_hi = dpi(P.pismall, (uint64_t) max_r);
+      if (O.i_hi > O.i_lo && xpq / P.primes[O.i_hi] < 6) O.mode = 6;
     }
     outs[qoff[j] + t] = O;
   }
@@ -456,6 +523,7 @@ __global__ void k_outer_C2(AcParams P, PairOuter* __restrict__ outs)
   if (min_m < max_m) {
     O.i_lo = dpi(P.pismall, (uint64_t) min_m);
     O.i_hi = dpi(P.pismall, (uint64_t) max_m);
+    if (O.i_hi > O.i_lo && xp / P.primes[O.i_hi] < 6) O.mode = 5;
   }
   outs[j] = O;
 }
