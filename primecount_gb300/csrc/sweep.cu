@@ -819,6 +819,9 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
         __syncthreads();
       }
       const int64_t total_e = loff[nb];
+      // FactorTable entries read: every record of the batch's levels is
+      // read once by the windows below (two-prime levels read primes instead)
+      if (tid < nb && !(lp[tid].flags & 2)) nentries += (unsigned long long) (loff[tid + 1] - loff[tid]);
 
       int li = 0;          // next batch level to finish
       int64_t w0 = 0;      // first flat record of the window
@@ -1069,16 +1072,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
             }
           }
         }
-        if (nrec > 0) {
-          if (tid == 0) {
-            for (int j = li; j < nb; j++) {
-              const int64_t a = dmax(loff[j], w0), e2 = dmin(loff[j + 1], wend);
-              if (a >= wend) break;
-              if (e2 > a && !(lp[j].flags & 2)) nentries += (unsigned long long) (e2 - a);
-            }
-          }
-          __syncthreads();
-        }
+        if (nrec > 0) __syncthreads();
         // ---- phase B: levels in order
         while (li < nb) {
           const int re = runend[li];
@@ -1105,8 +1099,22 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
           // against one bitmap state, then all their multiples crossed off at
           // once: one barrier pass instead of one per level.
           if ((lp[li].flags & 8) && loff[li] >= w0) {
-            int lj = li;
-            while (lj < nb && lj - li < A.group_max && (lp[lj].flags & 8) && loff[lj + 1] <= wend) lj++;
+            // lj: the first level from li on that cannot join the group, found
+            // by each warp's lanes checking 32 levels at once
+            int lj;
+            {
+              const int gm = A.group_max;
+              int j = li + lane;
+              bool no = !(j < nb && j - li < gm && (lp[j].flags & 8) && loff[j + 1] <= wend);
+              unsigned bal = __ballot_sync(0xffffffffu, no);
+              if (bal) lj = li + __ffs((int) bal) - 1;
+              else {
+                j += 32;
+                no = !(j < nb && j - li < gm && (lp[j].flags & 8) && loff[j + 1] <= wend);
+                bal = __ballot_sync(0xffffffffu, no);
+                lj = bal ? li + 32 + __ffs((int) bal) - 1 : li + 64;
+              }
+            }
             if (lj - li >= 2) {
               const int ra = (int) (loff[li] - w0), rb = (int) (loff[lj] - w0);
               if (tid < lj - li) {
@@ -1340,12 +1348,14 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
     for (int d = 16; d > 0; d >>= 1) {
       nleaves += __shfl_down_sync(0xffffffffu, nleaves, d);
       ntwo += __shfl_down_sync(0xffffffffu, ntwo, d);
+      nentries += __shfl_down_sync(0xffffffffu, nentries, d);
     }
     if (lane == 0) {
       if (nleaves) atomicAdd(&s_ctr[0], nleaves);
       if (ntwo) atomicAdd(&s_ctr[1], ntwo);
+      if (nentries) atomicAdd(&s_ctr[3], nentries);
     }
-    if (tid == 0) { atomicAdd(&s_ctr[2], (unsigned long long) Bs); atomicAdd(&s_ctr[3], nentries); }
+    if (tid == 0) atomicAdd(&s_ctr[2], (unsigned long long) Bs);
     __syncthreads();
     if (tid == 0) {
       long long t = 0;
