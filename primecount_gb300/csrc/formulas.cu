@@ -789,8 +789,8 @@ static int64_t ps_mid_div()
 {
   static const int64_t d = [] {
     const char* e = getenv("PCG_PS_MID");
-    const int64_t v = e ? atoll(e) : 512;
-    return v > 0 ? v : 512;
+    const int64_t v = e ? atoll(e) : 256;
+    return v > 0 ? v : 256;
   }();
   return d;
 }

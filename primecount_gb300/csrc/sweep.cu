@@ -551,6 +551,19 @@ __device__ __forceinline__ void block_scan3(long long v0, long long v1, long lon
   if (tid == NT - 1) { o0[NT] = e0 + v0; o1[NT] = e1 + v1; o2[NT] = e2 + v2; }
 }
 
+// the level j in [l0, l1) of flat record pos: loff[j] <= pos < loff[j + 1]
+// (loff[l0] <= pos < loff[l1]), by binary search
+static __device__ __forceinline__ int level_of(const int64_t* loff, int l0, int l1, int64_t pos)
+{
+  int j = l0;
+  for (int n = l1 - l0; n > 1;) {
+    const int half = n >> 1;
+    if (loff[j + half] <= pos) j += half;
+    n -= half;
+  }
+  return j;
+}
+
 template <typename FT, int NT>
 __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k_sweep(const SweepArgs A)
 {
@@ -1131,8 +1144,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                 for (int k2 = ra + warp; k2 < rb; k2 += NT / 32) {
                   const uint32_t r = rec[k2];
                   if (r == REC_NONE) continue;
-                  int lv = li;
-                  while (loff[lv + 1] <= w0 + k2) lv++;
+                  const int lv = level_of(loff, li, lj, w0 + k2);
                   const uint32_t off = r & 0x3FFFFFFFu;
                   const uint64_t n = (uint64_t) low + off;
                   const uint32_t wd = off / 240, ch = wd >> 3, kw = wd & 7;
@@ -1157,10 +1169,8 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                   }
                 }
               } else if (rb > ra) {
-                int lv = li;
                 for (int k2 = ra + tid; k2 < rb; k2 += NT) {
-                  const int64_t pos = w0 + k2;
-                  while (loff[lv + 1] <= pos) lv++;
+                  const int lv = level_of(loff, li, lj, w0 + k2);
                   const uint32_t r = rec[k2];
                   int sg = 0;
                   if (r != REC_NONE) {
