@@ -426,10 +426,29 @@ __device__ __forceinline__ void scan_chunks(const uint32_t* __restrict__ ccount,
   __syncthreads();
 }
 
+// the low nb bits set (nb in [0, 64]; the PTX shift clamps 64 to an empty result)
+static __device__ __forceinline__ uint64_t low_bits(uint32_t nb)
+{
+  uint64_t m;
+  asm("shr.b64 %0, %1, %2;" : "=l"(m) : "l"(~0ull), "r"(64u - nb));
+  return m;
+}
+
+// mask_le(r) from a shared table of the counts of wheel residues <= r
+static __device__ __forceinline__ uint64_t mask_le_t(const uint8_t* nbt, uint32_t r) { return low_bits(nbt[r]); }
+
+// dpi with the shared residue-count table
+static __device__ __forceinline__ int64_t dpi_t(const uint64_t* __restrict__ pt, const uint8_t* nbt, uint64_t x)
+{
+  if (x < 6) return (0x322100u >> (4 * x)) & 15u;
+  const uint64_t i = x / 240;
+  return (int64_t) (pt[2 * i] + __popcll(pt[2 * i + 1] & mask_le_t(nbt, (uint32_t) (x - 240 * i))));
+}
+
 // # unsieved numbers in [low, low + off]: the chunk prefix plus the popcounts
 // of the chunk's words up to the word of off, its 8 words read at once
 __device__ __forceinline__ uint32_t query(const uint64_t* __restrict__ bits, const uint32_t* __restrict__ pref,
-                                          uint32_t off)
+                                          const uint8_t* nbt, uint32_t off)
 {
   const uint32_t w = off / 240;
   const uint32_t r = off - w * 240;
@@ -437,7 +456,7 @@ __device__ __forceinline__ uint32_t query(const uint64_t* __restrict__ bits, con
   const uint32_t k = w & 7;
   const ulonglong2* q = (const ulonglong2*) (bits + (c << 3));
   const ulonglong2 w01 = q[0], w23 = q[1], w45 = q[2], w67 = q[3];
-  const uint64_t mk = mask_le(r);
+  const uint64_t mk = mask_le_t(nbt, r);
   auto part = [&](uint32_t i, uint64_t v) -> uint32_t {
     return (uint32_t) __popcll(i < k ? v : (i == k ? (v & mk) : 0ull));
   };
@@ -470,9 +489,9 @@ __device__ __forceinline__ uint32_t chunk_sum_below(const uint32_t* __restrict__
 // Cross off the number at offset w * 240 + rr of the segment: a 32-bit atomic
 // on the half of the 64-bit word that holds its bit (bits 0-31 of a word are
 // the lower half), true when the number was still unsieved
-__device__ __forceinline__ bool cross_off(uint64_t* bits, uint32_t w, uint32_t rr)
+__device__ __forceinline__ bool cross_off(uint64_t* bits, const uint8_t* bt, uint32_t w, uint32_t rr)
 {
-  const uint32_t bi = bit_of(rr);
+  const uint32_t bi = bt[rr];
   const uint32_t m = 1u << (bi & 31);
   return (atomicAnd((uint32_t*) bits + 2 * w + (bi >> 5), ~m) & m) != 0;
 }
@@ -484,7 +503,8 @@ __device__ __forceinline__ bool cross_off(uint64_t* bits, uint32_t w, uint32_t r
 // Different levels can share a half-word, so the clears are atomic.
 template <int NT>
 __device__ __forceinline__ void cross_off_levels(uint64_t* bits, uint32_t* ccount, const LevelP* lp,
-                                                 const int64_t* hoff, int l0, int l1, uint64_t low)
+                                                 const int64_t* hoff, int l0, int l1, uint64_t low,
+                                                 const uint8_t* bt)
 {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t h0 = hoff[l0], h1 = hoff[l1];
@@ -497,7 +517,7 @@ __device__ __forceinline__ void cross_off_levels(uint64_t* bits, uint32_t* ccoun
         const uint64_t q = 30 * (jj >> 3) + woff((uint32_t) (jj & 7));
         const uint32_t off = (uint32_t) (prime * q - low);
         const uint32_t w = off / 240, rr = off - w * 240;
-        if (cross_off(bits, w, rr)) atomicSub(&ccount[w >> 3], 1u);
+        if (cross_off(bits, bt, w, rr)) atomicSub(&ccount[w >> 3], 1u);
       }
     }
     return;
@@ -513,7 +533,7 @@ __device__ __forceinline__ void cross_off_levels(uint64_t* bits, uint32_t* ccoun
     const uint64_t q = 30 * (jj >> 3) + woff((uint32_t) (jj & 7));
     const uint32_t off = (uint32_t) ((uint64_t) Q.prime * q - low);
     const uint32_t w = off / 240, rr = off - w * 240;
-    if (cross_off(bits, w, rr)) atomicSub(&ccount[w >> 3], 1u);
+    if (cross_off(bits, bt, w, rr)) atomicSub(&ccount[w >> 3], 1u);
   }
 }
 
@@ -598,10 +618,16 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
   __shared__ unsigned long long s_ctr[5];
 
   __shared__ SweepQ s_q;                               // the problem of the current segment
+  __shared__ uint8_t s_nb[240];                        // # wheel residues <= r, r in [0, 240)
+  __shared__ uint8_t s_bitt[240];                      // bit of residue r in its 64-bit word (r coprime to 30)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int cap = A.rec_cap;
   const FT* __restrict__ factor = (const FT*) A.factor;
   for (int i = tid; i < 480; i += NT) cop[i] = A.coprime[i];
+  for (int i = tid; i < 240; i += NT) {
+    s_nb[i] = (uint8_t) ((i / 30) * 8 + cnt8((uint32_t) (i % 30)));
+    s_bitt[i] = (uint8_t) bit_of((uint32_t) i);
+  }
   // wheel patterns: word r of prime p keeps the numbers 240 r + {1,7,..,29}
   // (mod 240 p) that p does not divide
   for (int i = tid; i < PAT_WORDS; i += NT) {
@@ -1088,7 +1114,10 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
         if (nrec > 0) __syncthreads();
         // ---- phase B: levels in order
         while (li < nb) {
+          // the level's shared-memory fields, loaded together
           const int re = runend[li];
+          const uint32_t lflags = lp[li].flags;
+          const int64_t la = loff[li], lz = loff[li + 1];
           if (re > li) {
             // a run of leafless levels li .. re-1 with formula counts: their
             // counts from the prefix, all their multiples crossed off at once
@@ -1096,7 +1125,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
             for (int t = tid; t < re - li; t += NT)
               A.cnt[rowbase + b0 + li + t] = total - (uint32_t) (rpre[li + t] - r0);
             const int64_t h0 = hoff[li], h1 = hoff[re];
-            cross_off_levels<NT>(bits, ccount, lp, hoff, li, re, (uint64_t) low);
+            cross_off_levels<NT>(bits, ccount, lp, hoff, li, re, (uint64_t) low, s_bitt);
             const uint32_t removed = (uint32_t) (rpre[re] - r0);
             total -= removed;
             if (h1 > h0) dirty = true;
@@ -1111,7 +1140,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
           // pi(n / p_b) - pi(q_lo_b - 1)).  All their records are answered
           // against one bitmap state, then all their multiples crossed off at
           // once: one barrier pass instead of one per level.
-          if ((lp[li].flags & 8) && loff[li] >= w0) {
+          if ((lflags & 8) && la >= w0) {
             // lj: the first level from li on that cannot join the group, found
             // by each warp's lanes checking 32 levels at once
             int lj;
@@ -1152,13 +1181,13 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                   if (lane < 8) {
                     const uint64_t v = bits[8 * ch + lane];
                     const uint32_t j = (uint32_t) lane;
-                    part += (uint32_t) __popcll(j < kw ? v : (j == kw ? (v & mask_le(off - wd * 240)) : 0ull));
+                    part += (uint32_t) __popcll(j < kw ? v : (j == kw ? (v & mask_le_t(s_nb, off - wd * 240)) : 0ull));
                   }
                   // the numbers <= n removed by the levels li .. lv-1, one per lane
                   for (int b = li + lane; b < lv; b += 32) {
                     const uint64_t pb = lp[b].prime;
                     if (pb <= n && pb >= (uint64_t) low) part--;
-                    const int64_t d = dpi(A.pitab, div_magic(n, pb, s_gmag[b - li])) - (int64_t) s_pc[b];
+                    const int64_t d = dpi_t(A.pitab, s_nb, div_magic(n, pb, s_gmag[b - li])) - (int64_t) s_pc[b];
                     if (d > 0) part -= (uint32_t) d;
                   }
                   // the count is below 2^32: the sum modulo 2^32 is exact
@@ -1175,7 +1204,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                   int sg = 0;
                   if (r != REC_NONE) {
                     const uint32_t off = r & 0x3FFFFFFFu;
-                    uint32_t c = query(bits, pref, off);
+                    uint32_t c = query(bits, pref, s_nb, off);
                     const uint64_t n = (uint64_t) low + off;
                     // four levels at a time: their PiTable words are loaded together
                     int b = li;
@@ -1193,7 +1222,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
 #pragma unroll
                       for (int u = 0; u < 4; u++) {
                         // for t < 6 this reads 3 + a few bits, still below s_pc[b] >= pi(63): dropped by d > 0
-                        const int64_t pt = (int64_t) (e[u].x + __popcll(e[u].y & mask_le((uint32_t) (t[u] % 240))));
+                        const int64_t pt = (int64_t) (e[u].x + __popcll(e[u].y & mask_le_t(s_nb, (uint32_t) (t[u] % 240))));
                         const int64_t d = pt - (int64_t) s_pc[b + u];
                         if (d > 0) c -= (uint32_t) d;
                       }
@@ -1201,7 +1230,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                     for (; b < lv; b++) {
                       const uint64_t pb = lp[b].prime;
                       if (pb <= n && pb >= (uint64_t) low) c--;
-                      const int64_t d = dpi(A.pitab, div_magic(n, pb, s_gmag[b - li])) - (int64_t) s_pc[b];
+                      const int64_t d = dpi_t(A.pitab, s_nb, div_magic(n, pb, s_gmag[b - li])) - (int64_t) s_pc[b];
                       if (d > 0) c -= (uint32_t) d;
                     }
                     if (r & (1u << 30)) { lsum -= c; sg = -1; }
@@ -1224,7 +1253,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
               }
               // all their multiples crossed off at once
               const int64_t h0 = hoff[li], h1 = hoff[lj];
-              cross_off_levels<NT>(bits, ccount, lp, hoff, li, lj, (uint64_t) low);
+              cross_off_levels<NT>(bits, ccount, lp, hoff, li, lj, (uint64_t) low, s_bitt);
               total -= (uint32_t) (rpre[lj] - r0);
               if (h1 > h0) dirty = true;
               li = lj;
@@ -1232,7 +1261,6 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
               continue;
             }
           }
-          const int64_t la = loff[li], lz = loff[li + 1];
           if (lz > la && la >= wend) break;               // records start in a later window
           const int l = b0 + li;
           if (la >= w0 && tid == 0) A.cnt[rowbase + l] = total;
@@ -1254,7 +1282,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                 if (lane < 8) {
                   const uint64_t v = bits[8 * ch + lane];
                   const uint32_t j = (uint32_t) lane;
-                  part += (uint32_t) __popcll(j < kw ? v : (j == kw ? (v & mask_le(off - wd * 240)) : 0ull));
+                  part += (uint32_t) __popcll(j < kw ? v : (j == kw ? (v & mask_le_t(s_nb, off - wd * 240)) : 0ull));
                 }
                 const uint32_t c = __reduce_add_sync(0xffffffffu, part);
                 if (r & (1u << 30)) { if (lane == 0) lsum -= c; smu_w--; }
@@ -1268,7 +1296,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                 for (int k2 = ra + tid; k2 < rb; k2 += NT) {
                   const uint32_t r = rec[k2];
                   if (r != REC_NONE) {
-                    const uint32_t c = query(bits, pref, r & 0x3FFFFFFFu);
+                    const uint32_t c = query(bits, pref, s_nb, r & 0x3FFFFFFFu);
                     if (r & (1u << 30)) { lsum -= c; smu_t--; }
                     else { lsum += c; smu_t++; }
                   }
@@ -1283,8 +1311,10 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
           if (lz > wend) break;                            // the level continues in the next window
           // ---- cross off p_l and its multiples, count the numbers removed first
           const LevelP& P = lp[li];
+          const uint32_t pjn = P.jn, pprime = P.prime;
+          const uint64_t pjlo = P.jlo;
           uint32_t rem = 0;
-          if (P.flags & 4) {
+          if (lflags & 4) {
             // small prime: AND with its wheel pattern, one owner thread per word
             const uint32_t p = P.prime;
             int po = 0;
@@ -1313,31 +1343,31 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
               r += step;
               if (r >= p) r -= p;
             }
-          } else if (P.jn) {
-            if ((uint32_t) tid < P.jn) {
+          } else if (pjn) {
+            if ((uint32_t) tid < pjn) {
               // co-factors tid, tid + NT, ...: NT / 8 wheel turns apart, so
               // the multiples are NT p / 64 words apart with the same bit
-              const uint64_t p = P.prime;
-              const uint64_t jj = P.jlo + (uint64_t) tid;
+              const uint64_t p = pprime;
+              const uint64_t jj = pjlo + (uint64_t) tid;
               const uint64_t q = 30 * (jj >> 3) + woff((uint32_t) (jj & 7));
               const uint32_t off = (uint32_t) (p * q - (uint64_t) low);
               const uint32_t w = off / 240;
-              const uint32_t bi = bit_of(off - w * 240);
+              const uint32_t bi = s_bitt[off - w * 240];
               const uint32_t m = 1u << (bi & 31);
               // the number's 32-bit half-word, and the half-word stride
               uint32_t h = 2 * w + (bi >> 5);
               const uint32_t hstep = (uint32_t) p * (NT / 32);
               uint32_t* const hw = (uint32_t*) bits;
-              for (uint32_t j = tid; j < P.jn; j += NT, h += hstep) {
+              for (uint32_t j = tid; j < pjn; j += NT, h += hstep) {
                 const uint32_t old = hw[h];
                 if (old & m) { hw[h] = old & ~m; rem++; atomicSub(&ccount[h >> 4], 1u); }
               }
             }
           }
-          if (P.flags & 8) {
+          if (lflags & 8) {
             __syncthreads();
             total -= P.fcount;
-            if (P.jn) dirty = true;
+            if (pjn) dirty = true;
           } else {
             rem = __reduce_add_sync(0xffffffffu, rem);
             if (lane == 0 && rem) atomicAdd(&s_rem[l % 3], rem);
