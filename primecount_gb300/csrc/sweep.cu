@@ -1263,7 +1263,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
           }
           if (lz > la && la >= wend) break;               // records start in a later window
           const int l = b0 + li;
-          if (la >= w0 && tid == 0) A.cnt[rowbase + l] = total;
+          if (la >= w0 && tid == NT - 1) A.cnt[rowbase + l] = total;   // the last thread: rarely a multiple to cross off
           const int ra = (int) (dmax(la, w0) - w0);
           const int rz = (int) (dmin(lz, wend) - w0);           // end of the level's window records
           const int rb = li == clev ? s_ncomp[win & 1] : rz;   // end of those still to answer
@@ -1307,7 +1307,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
             }
             __syncthreads();
           }
-          if (rz > ra && lz <= wend && tid == 0) { A.smu[rowbase + l] = s_smu; s_smu = 0; }
+          if (rz > ra && lz <= wend && tid == NT - 1) { A.smu[rowbase + l] = s_smu; s_smu = 0; }
           if (lz > wend) break;                            // the level continues in the next window
           // ---- cross off p_l and its multiples, count the numbers removed first
           const LevelP& P = lp[li];
@@ -1368,6 +1368,12 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
             __syncthreads();
             total -= P.fcount;
             if (pjn) dirty = true;
+          } else if (!(lflags & 4) && pjn <= (uint32_t) NT) {
+            // at most one multiple per thread: the barrier counts the removals
+            const uint32_t rr = (uint32_t) __syncthreads_count(rem != 0);
+            total -= rr;
+            if (rr) dirty = true;
+            if (tid == NT - 1) s_rem[(l + 2) % 3] = 0;
           } else {
             rem = __reduce_add_sync(0xffffffffu, rem);
             if (lane == 0 && rem) atomicAdd(&s_rem[l % 3], rem);
@@ -1375,7 +1381,7 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
             const uint32_t rr = s_rem[l % 3];
             total -= rr;
             if (rr) dirty = true;
-            if (tid == 0) s_rem[(l + 2) % 3] = 0;
+            if (tid == NT - 1) s_rem[(l + 2) % 3] = 0;
           }
           li++;
         }
