@@ -776,9 +776,11 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
             if (b <= PQ.pi_sqrt) {
               int64_t min_m, max_m;
               if (PQ.gourdon == 2) {
-                // phi(x, a): m in (max(y / p, x / (p high)), min(y, x / (p low))]
+                // phi(x, a): m in (max(y / p, x / (p high), p), min(y, x / (p low))]; the
+                // bound m > p matters once p^2 > y, where the primes m in (y / p, p]
+                // would pass the table's filter (a prime's entry is T_MAX)
                 int64_t xp_high = divcap_m(xp, (uint64_t) high, s_mhigh, PQ.y);
-                min_m = dmax(xp_high, (int64_t) div_magic((uint64_t) PQ.y, p, pm));
+                min_m = dmax(dmax(xp_high, (int64_t) div_magic((uint64_t) PQ.y, p, pm)), prime);
                 max_m = divcap_m(xp, (uint64_t) low1, s_mlow, PQ.y);
                 P.thr = (uint32_t) (2 * b + 1);
               } else if (PQ.gourdon) {
@@ -1830,7 +1832,7 @@ static bool plan_segments_core(const SweepProblem& pb, const Tables& t, int64_t 
     for (int64_t b = pb.k + 1; b <= bglob; b++) {
       const double p = (double) t.h_primes[(size_t) b], xp = x / p;
       double mlo, mhi;
-      if (pb.gourdon == 2) { mlo = std::max(y / p, xp / hi); mhi = std::min(xp / l1, y); }
+      if (pb.gourdon == 2) { mlo = std::max({y / p, xp / hi, p}); mhi = std::min(xp / l1, y); }
       else if (pb.gourdon) {
         if (b <= pi_sqrt) { mlo = std::max(z / p, xp / hi); mhi = std::min({xp / (p * p), z, xp / l1}); }
         else { mlo = std::max(p, xp / hi); mhi = std::min({xp / (p * p), y, xp / l1}); }

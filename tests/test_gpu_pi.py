@@ -74,6 +74,15 @@ def test_phi_all_regimes_against_oracle(pcg, ora):
         assert pcg.phi(x, a) == ora.phi(x, a), (x, a)
 
 
+def test_phi_special_leaves_beyond_sqrt_y(pcg, ora):
+    # the special-leaf regime (8 < a, p_{a+1}^4 <= x) where p_a^2 exceeds the leaf
+    # bound y: the levels with p_b^2 > y need m > p_b besides m > y / p_b
+    # (43463692470, 78) is query 3976 of the seeded phi batch
+    for x, a in [(3 * 10 ** 8, 30), (10 ** 9, 30), (2 * 10 ** 9, 30), (8 * 10 ** 9, 60), (10 ** 10, 60),
+                 (43463692470, 78), (30000000000, 78)]:
+        assert pcg.phi(x, a) == ora.phi(x, a), (x, a)
+
+
 @pytest.mark.gpu
 def test_pi_other_alpha(pcg, golden):
     """pi(x) does not depend on Gourdon's y and z: other alpha_y / alpha_z (the
