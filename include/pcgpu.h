@@ -256,6 +256,15 @@ pcg_status pcg_pi(pcg_i128 x, const pcg_opts* opts, pcg_i128* out);
  * Sigma, pi(x)} with pi = (A + C) - B + D + Phi0 + Sigma (the reference's
  * --AC, --B, --D, --Phi0, --Sigma options, src/app/main.cpp:465-579). */
 pcg_status pcg_pi_terms(pcg_i128 x, const pcg_opts* opts, pcg_i128* out6);
+/* pi(x) by the Deleglise-Rivat formula (pi_deleglise_rivat_64/128,
+ * src/deleglise-rivat/pi_deleglise_rivat.cpp:61-136; the reference's -d
+ * option): pi(y) + S1 + S2_trivial + S2_easy + S2_hard - 1 - P2, S2_hard by
+ * the engine.  x <= 1e10 is counted by a sieve. */
+pcg_status pcg_pi_deleglise_rivat(pcg_i128 x, const pcg_opts* opts, pcg_i128* out);
+/* Its terms for x > 1e10: out7 = {S1, S2_trivial, S2_easy, S2_hard, P2,
+ * pi(y), pi(x)} (the reference's --S1, --S2-trivial, --S2-easy, --S2-hard,
+ * --P2 options, src/app/main.cpp:325-461), y, z, c as pcg_dr_params. */
+pcg_status pcg_pi_dr_terms(pcg_i128 x, const pcg_opts* opts, pcg_i128* out7);
 /* phi(x, a): numbers <= x not divisible by any of the first a primes. */
 pcg_status pcg_phi(int64_t x, int64_t a, const pcg_opts* opts, int64_t* out);
 

@@ -100,6 +100,10 @@ def load(path=None):
     L.pcg_phi.argtypes = [c_i64, c_i64, c_p(Opts), c_p(c_i64)]
     L.pcg_pi_terms.argtypes = [I128, c_p(Opts), c_p(I128)]
     L.pcg_pi_terms.restype = ctypes.c_int
+    L.pcg_pi_deleglise_rivat.argtypes = [I128, c_p(Opts), c_p(I128)]
+    L.pcg_pi_deleglise_rivat.restype = ctypes.c_int
+    L.pcg_pi_dr_terms.argtypes = [I128, c_p(Opts), c_p(I128)]
+    L.pcg_pi_dr_terms.restype = ctypes.c_int
     L.pcg_pi_batch.argtypes = [c_p(I128), ctypes.c_size_t, c_p(I128), c_p(Opts)]
     L.pcg_phi_batch.argtypes = [c_p(c_i64), c_p(c_i64), ctypes.c_size_t, c_p(c_i64), c_p(Opts)]
     L.pcg_ctx_create.argtypes = [I128, ctypes.c_uint64, c_p(ctypes.c_void_p)]
@@ -296,6 +300,27 @@ def pi_terms(x, ctx=None, stream=None, alpha_y=0.0, alpha_z=0.0):
     _check(load().pcg_pi_terms(to_i128(x), ctypes.byref(o), out), ctx)
     v = [from_i128(t) for t in out]
     return dict(zip(("AC", "B", "D", "Phi0", "Sigma", "pi"), v))
+
+
+def pi_deleglise_rivat(x, threads=0, print=False, ctx=None, stream=None):
+    """Number of primes <= x by the Deleglise-Rivat formula (the reference's
+    pi_deleglise_rivat, option -d): S2_hard on the engine, the other terms on
+    the device as well."""
+    out = I128()
+    o = _opts(ctx, stream, threads, print)
+    _check(load().pcg_pi_deleglise_rivat(to_i128(x), ctypes.byref(o), ctypes.byref(out)), ctx)
+    return from_i128(out)
+
+
+def pi_dr_terms(x, ctx=None, stream=None):
+    """The terms of the Deleglise-Rivat formula for x > 1e10 (the reference's
+    --S1, --S2-trivial, --S2-easy, --S2-hard, --P2 options): dict with S1,
+    S2_trivial, S2_easy, S2_hard, P2, pi_y and pi."""
+    out = (I128 * 7)()
+    o = _opts(ctx, stream)
+    _check(load().pcg_pi_dr_terms(to_i128(x), ctypes.byref(o), out), ctx)
+    v = [from_i128(t) for t in out]
+    return dict(zip(("S1", "S2_trivial", "S2_easy", "S2_hard", "P2", "pi_y", "pi"), v))
 
 
 def phi(x, a, threads=0, ctx=None, stream=None):

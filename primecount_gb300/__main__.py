@@ -6,6 +6,8 @@ serves:
     python -m primecount_gb300 1e20 --D              D(x) with the default y, z, k
     python -m primecount_gb300 1e18 --S2-hard        S2_hard(x) with the default y, z, c
     python -m primecount_gb300 1e20 --AC | --B | --Phi0 | --Sigma
+    python -m primecount_gb300 1e20 -d               pi(x) by the Deleglise-Rivat algorithm
+    python -m primecount_gb300 1e20 --S1 | --S2-trivial | --S2-easy | --P2
     python -m primecount_gb300 1e12 78498 --phi      phi(x, a)
     options: -s / --status (print the parameters), --time, -t / --threads N,
              --alpha-y=A, --alpha-z=A (Gourdon's y = A x^(1/3), z = A y for pi(x))
@@ -52,7 +54,10 @@ def parse_number(s):
 
 
 OPTIONS = {"--D": "D", "-D": "D", "--S2-hard": "S2_hard", "--AC": "AC", "--B": "B", "-B": "B",
-           "--Phi0": "Phi0", "--Sigma": "Sigma", "--phi": "phi", "-g": "pi", "--gourdon": "pi"}
+           "--Phi0": "Phi0", "--Sigma": "Sigma", "--phi": "phi", "-g": "pi", "--gourdon": "pi",
+           "-d": "dr", "--deleglise-rivat": "dr", "--S1": "S1", "--S2-trivial": "S2_trivial",
+           "--S2-easy": "S2_easy", "--P2": "P2"}
+DR_TERMS = ("S1", "S2_trivial", "S2_easy", "P2")
 
 
 def main(argv=None):
@@ -108,6 +113,18 @@ def main(argv=None):
             p = pcg.gourdon_params(x)
             print("x = %d\ny = %d\nz = %d\nk = %d\nx_star = %d" % (x, p["y"], p["z"], p["k"], p["x_star"]))
         r = pcg.pi(x, threads=threads, alpha_y=alpha_y, alpha_z=alpha_z)
+    elif option == "dr":
+        if status and x > 10 ** 10:
+            p = pcg.dr_params(x)
+            print("x = %d\ny = %d\nz = %d\nc = %d" % (x, p["y"], p["z"], p["c"]))
+        r = pcg.pi_deleglise_rivat(x, threads=threads)
+    elif option in DR_TERMS:
+        if x <= 10 ** 10:
+            raise pcg.PrimecountError(1, "--%s: the formula terms are computed for x > 1e10" % option.replace("_", "-"))
+        if status:
+            p = pcg.dr_params(x)
+            print("x = %d\ny = %d\nz = %d\nc = %d" % (x, p["y"], p["z"], p["c"]))
+        r = pcg.pi_dr_terms(x)[option]
     else:
         if x <= 10 ** 10:
             raise pcg.PrimecountError(1, "--%s: the formula terms are computed for x > 1e10" % option)

@@ -528,6 +528,37 @@ __global__ void k_outer_C2(AcParams P, PairOuter* __restrict__ outs)
   outs[j] = O;
 }
 
+// S2_easy outers (Deleglise-Rivat, S2_easy.cpp:60-140): b in (b0, b1] =
+// (max(c, pi(sqrt y)), pi(x^(1/3))], the primes q = primes[i] with i in
+// (pi(in_between(p, z / p, y)), pi(min(x / p^2, y))]; term pi(x / (p q)) - b + 2.
+// The reference's clustered leaves (equal successive terms) are the same terms.
+__global__ void k_outer_S2e(uint64_t x_lo, uint64_t x_hi, int64_t y, int64_t z, int64_t b0, int64_t b1,
+                            const uint32_t* __restrict__ primes, const uint64_t* __restrict__ pismall,
+                            PairOuter* __restrict__ outs)
+{
+  const int64_t j = (int64_t) blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t b = b0 + 1 + j;
+  if (b > b1) return;
+  const u128 x = ((u128) x_hi << 64) | x_lo;
+  const uint64_t p = primes[b];
+  const u128 xp = div128(x, p);
+  const u128 xpp = xp / p;
+  const int64_t min_trivial = xpp < (u128) y ? (int64_t) xpp : y;
+  int64_t min_sparse = z / (int64_t) p;
+  if (min_sparse < (int64_t) p || y < (int64_t) p) min_sparse = (int64_t) p;
+  else if (min_sparse > y) min_sparse = y;
+  PairOuter O;
+  O.xp_lo = (uint64_t) xp;
+  O.xp_hi = (uint64_t) (xp >> 64);
+  O.cap = 0;
+  O.b = (int32_t) b;
+  O.mode = 1;
+  O.i_hi = dpi(pismall, (uint64_t) min_trivial);
+  O.i_lo = dpi(pismall, (uint64_t) min_sparse);
+  if (O.i_hi < O.i_lo) O.i_hi = O.i_lo;
+  outs[j] = O;
+}
+
 // ---------------------------------------------------------------- prime sieve segments (B, small pi)
 // Each CTA sieves a segment [lo, hi) (lo a multiple of 240) of the numbers
 // coprime to 30, leaving the primes.  Mode count: seg_c[s] = # primes >= 7 in
@@ -943,6 +974,28 @@ static cudaStream_t aux_stream(Ctx& c)
   return c.aux;
 }
 
+// sum over the primes y < p <= sqrt(x) of pi(x / p): Gourdon's B (B.cpp:38-131)
+// and, less the arithmetic series of the prime indices, Deleglise-Rivat's P2
+// (P2.cpp).  A prime sieve of [x / sqrt(x), x / y] answers the queries x / p
+// in each segment; the segments are joined by the running count pi(lo - 1).
+static i128 sum_pi_x_over_p(Ctx& c, u128 x, int64_t y, int64_t sqrtx, cudaStream_t s, uint64_t* nl)
+{
+  const int64_t n0 = (int64_t) (x / (u128) sqrtx);        // smallest x / p
+  const int64_t n1 = (int64_t) (x / (u128) (y + 1)) + 1;  // x / p < n1 for p > y
+  i128 B = 0;
+  if (sqrtx > y && n1 > n0) {
+    PsOut o = run_psieve(c, x, n0, n1, true, y, sqrtx, s, nl);
+    // pi(lo0 - 1) from the PiTable up to sqrt(x) (lo0 >= sqrt(x) > 1e5 here)
+    i128 run = 0;
+    if (o.lo0 >= 7) run = pi_lookup(c, std::vector<uint64_t>{(uint64_t) (o.lo0 - 1)}, s)[0];
+    for (int64_t i = 0; i < o.nseg; i++) {
+      B += (i128) o.l[(size_t) i] + (i128) o.m[(size_t) i] * run;
+      run += o.c[(size_t) i];
+    }
+  }
+  return B;
+}
+
 // with_d = false leaves D out (R.d = 0, R.pi without it): the batch form
 // computes the D of all its queries in one batched sweep
 static PiParts pi_gourdon(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s, bool with_d = true)
@@ -1048,20 +1101,7 @@ static PiParts pi_gourdon(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s, bo
     // ---- B = sum over primes y < p <= sqrt(x) of pi(x / p)
     {
       double t1 = fnow_ms();
-      const int64_t n0 = (int64_t) (x / (u128) sqrtx);   // smallest x / p
-      const int64_t n1 = (int64_t) (x / (u128) (y + 1)) + 1;  // x / p < n1 for p > y
-      i128 B = 0;
-      if (sqrtx > y && n1 > n0) {
-        PsOut o = run_psieve(c, x, n0, n1, true, y, sqrtx, s, nl);
-        // pi(lo0 - 1) from the PiTable up to sqrt(x) (lo0 >= sqrt(x) > 1e5 here)
-        i128 run = 0;
-        if (o.lo0 >= 7) run = pi_lookup(c, std::vector<uint64_t>{(uint64_t) (o.lo0 - 1)}, s)[0];
-        for (int64_t i = 0; i < o.nseg; i++) {
-          B += (i128) o.l[(size_t) i] + (i128) o.m[(size_t) i] * run;
-          run += o.c[(size_t) i];
-        }
-      }
-      R.b = B;
+      R.b = sum_pi_x_over_p(c, x, y, sqrtx, s, nl);
       R.ms_b = fnow_ms() - t1;
     }
 
@@ -1155,6 +1195,120 @@ static PiParts pi_gourdon(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s, bo
   R.launches += launches2;
   R.pi = R.ac - R.b + R.d + R.phi0 + R.sigma;
   return R;
+}
+
+// ---- pi(x) by the Deleglise-Rivat formula (pi_deleglise_rivat.cpp:61-136):
+// pi(x) = pi(y) + S1 + S2_trivial + S2_easy + S2_hard - 1 - P2 with y =
+// alpha x^(1/3), z = x / y, c = PhiTiny::get_c(y).  out7 = {S1, S2_trivial,
+// S2_easy, S2_hard, P2, pi(y), pi(x)}.  S2_hard is the engine's sweep; S1 the
+// ordinary leaves over the FactorTable; S2_easy the pair-sum kernel;
+// S2_trivial closed forms on the host; P2 the prime sieve of B.
+void pi_dr_terms(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s, i128 out[7])
+{
+  const DrParams g = dr_params(x);
+  const int64_t y = g.y, z = g.z, cc = g.c;
+  if (x > ((u128) y << 62)) fail(PCG_ERANGE, "pi_deleglise_rivat(x): x is too large");
+  const int64_t sqrtx = isqrt(x);
+  const int64_t x13 = iroot(x, 3);
+  ensure_prime_tables(c, std::max<int64_t>(y, 1000), s);
+  ensure_factor_dr(c, y, s);
+  ensure_pibig(c, sqrtx + 240, s);
+  ensure_phi_tiny(c, (int) cc, s);
+  const Tables& T = c.tab;
+  const int64_t pi_y = host_pi(T, (uint64_t) y);
+  const int64_t prime_c = T.h_primes[(size_t) cc];
+
+  // S2_hard (S2_hard.cpp:221-293): the sweep
+  i128 s2_hard;
+  {
+    SweepProblem p;
+    p.gourdon = 0;
+    p.x = x;
+    p.y = y;
+    p.z = z;
+    p.k = cc;
+    s2_hard = run_sweep(c, p, tune, s).sum;
+  }
+
+  // S1 (S1.cpp): sum over the square-free n <= y with lpf(n) > p_c of
+  // mu(n) phi(x / n, c): the FactorTable entries above p_c (1 -> T_MAX - 1,
+  // composites lpf or lpf - 1 by mu, primes T_MAX) except the primes <= p_c
+  i128 s1;
+  {
+    const int64_t size = wheel2310().to_index((uint64_t) y) + 1;
+    const int grid = c.num_sms * 8;
+    DevBuf& part = c.tmp[T_PHI0_PART];
+    part.alloc((size_t) grid * 16);
+    PCG_CUDA(cudaMemsetAsync(part.p, 0, (size_t) grid * 16, s));
+    PhiTab PT = phi_tab(c);
+    if (T.fr_bytes == 2)
+      k_phi0<uint16_t><<<grid, 256, 0, s>>>((uint64_t) x, (uint64_t) (x >> 64), T.factor_dr.as<uint16_t>(), size,
+                                            (uint32_t) prime_c, (uint64_t) prime_c, PT, T.coprime.as<uint16_t>(),
+                                            part.as<i128>());
+    else
+      k_phi0<uint32_t><<<grid, 256, 0, s>>>((uint64_t) x, (uint64_t) (x >> 64), T.factor_dr.as<uint32_t>(), size,
+                                            (uint32_t) prime_c, (uint64_t) prime_c, PT, T.coprime.as<uint16_t>(),
+                                            part.as<i128>());
+    PCG_CUDA(cudaGetLastError());
+    s1 = sum_partials(part, grid, s);
+  }
+
+  // S2_trivial (S2_trivial.cpp:34-88): the leaves p_b p_l with phi(x / n, b - 1) = 1
+  i128 s2_trivial = 0;
+  if (y >= 2) {
+    const int64_t start = std::max<int64_t>(prime_c, isqrt((u128) z)) + 1;
+    if (start < y) {
+      int64_t j = host_pi(T, (uint64_t) (start - 1)) + 1;
+      int64_t prime = INT64_MAX;
+      for (; j <= T.nprimes; j++) {
+        prime = T.h_primes[(size_t) j];
+        if (prime >= y) break;
+        const int64_t xpp = (int64_t) (x / ((u128) prime * (u128) prime));
+        if (xpp <= prime) break;
+        s2_trivial += (i128) (pi_y - host_pi(T, (uint64_t) xpp));
+      }
+      if (j > T.nprimes) prime = INT64_MAX;
+      if (prime < y) {
+        const i128 n = (i128) (host_pi(T, (uint64_t) (y - 1)) - host_pi(T, (uint64_t) prime)) + 1;
+        const i128 a1 = (i128) (pi_y - host_pi(T, (uint64_t) (y - 1)));
+        const i128 a2 = (i128) (pi_y - host_pi(T, (uint64_t) prime));
+        s2_trivial += n * (a1 + a2) / 2;
+      }
+    }
+  }
+
+  // S2_easy (S2_easy.cpp): pair sums pi(x / (p_b q)) - b + 2
+  i128 s2_easy = 0;
+  {
+    const int64_t b0 = std::max<int64_t>(cc, host_pi(T, (uint64_t) isqrt((u128) y)));
+    const int64_t b1 = host_pi(T, (uint64_t) x13);
+    const int64_t n = std::max<int64_t>(0, b1 - b0);
+    if (n > 0) {
+      DevBuf& outs = c.tmp[T_AC_OUTS];
+      outs.alloc((size_t) n * sizeof(PairOuter));
+      k_outer_S2e<<<(unsigned) ((n + 127) / 128), 128, 0, s>>>((uint64_t) x, (uint64_t) (x >> 64), y, z, b0, b1,
+                                                              T.primes.as<uint32_t>(), T.pitab.as<uint64_t>(),
+                                                              outs.as<PairOuter>());
+      PCG_CUDA(cudaGetLastError());
+      s2_easy = run_pairs(c, outs.as<PairOuter>(), n, s, nullptr);
+    }
+  }
+
+  // P2 (P2.cpp): sum over y < p <= sqrt(x) of pi(x / p) - pi(p) + 1
+  i128 p2;
+  {
+    const i128 B = sum_pi_x_over_p(c, x, y, sqrtx, s, nullptr);
+    const i128 n2 = pi_lookup(c, std::vector<uint64_t>{(uint64_t) sqrtx}, s)[0];   // PiTable up to sqrt(x)
+    const i128 a = pi_y;
+    p2 = sqrtx > y ? B - (n2 * (n2 - 1) - a * (a - 1)) / 2 : 0;
+  }
+  out[0] = s1;
+  out[1] = s2_trivial;
+  out[2] = s2_easy;
+  out[3] = s2_hard;
+  out[4] = p2;
+  out[5] = pi_y;
+  out[6] = (i128) pi_y + s1 + s2_trivial + s2_easy + s2_hard - 1 - p2;
 }
 
 // x <= 1e10 is counted by the sieve directly

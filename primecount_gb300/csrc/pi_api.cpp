@@ -14,6 +14,7 @@ namespace pcg {
 i128 pi_any(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s, pcg_stats* st);
 i128 pi_without_d(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s, bool* needs_d);
 void pi_gourdon_terms(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s, i128 out[6]);
+void pi_dr_terms(Ctx& c, u128 x, const Tuning& tune, cudaStream_t s, i128 out[7]);
 int64_t phi_any(Ctx& c, int64_t x, int64_t a, const Tuning& tune, cudaStream_t s);
 }  // namespace pcg
 
@@ -53,6 +54,36 @@ pcg_status pcg_pi(pcg_i128 xi, const pcg_opts* opts, pcg_i128* out)
     c.last = st;
     if (opts && opts->print) std::printf("pi(x) = %s\nSeconds: %.3f\n", to_string(r).c_str(), st.total_ms / 1000);
     *out = to_pcg(r);
+  });
+}
+
+pcg_status pcg_pi_deleglise_rivat(pcg_i128 xi, const pcg_opts* opts, pcg_i128* out)
+{
+  if (!out) return PCG_EINVAL;
+  return pcg_guarded(opts, [&](Ctx& c, cudaStream_t s) {
+    if (xi.hi < 0) { *out = to_pcg(0); return; }       // pi(x) = 0 for x < 2
+    const u128 x = make_u128(xi);
+    if (x <= (u128) 10000000000ull) {                  // small x: counted by the sieve, as pcg_pi does
+      *out = to_pcg(pi_any(c, x, tune_of(opts), s, nullptr));
+      return;
+    }
+    i128 t[7];
+    pi_dr_terms(c, x, tune_of(opts), s, t);
+    if (opts && opts->print) std::printf("pi(x) = %s\n", to_string(t[6]).c_str());
+    *out = to_pcg(t[6]);
+  });
+}
+
+pcg_status pcg_pi_dr_terms(pcg_i128 xi, const pcg_opts* opts, pcg_i128* out7)
+{
+  if (!out7) return PCG_EINVAL;
+  return pcg_guarded(opts, [&](Ctx& c, cudaStream_t s) {
+    if (xi.hi < 0) fail(PCG_EINVAL, "x must be >= 0");
+    const u128 x = make_u128(xi);
+    if (x <= (u128) 10000000000ull) fail(PCG_EINVAL, "pcg_pi_dr_terms needs x > 1e10 (smaller x is counted by a sieve)");
+    i128 t[7];
+    pi_dr_terms(c, x, tune_of(opts), s, t);
+    for (int i = 0; i < 7; i++) out7[i] = to_pcg(t[i]);
   });
 }
 

@@ -65,7 +65,7 @@ def run_status(x, opt):
     lines = [l for l in out.splitlines() if l.strip()]
     res = int(lines[-1]) if re.fullmatch(r"-?\d+", lines[-1].strip()) else None
     if res is None:
-        m = re.findall(r"^(?:D|S2_hard|A \+ C|B|Phi0|Sigma) = (-?\d+)$", out, re.M)
+        m = re.findall(r"^(?:D|S2_hard|A \+ C|B|Phi0|Sigma|S1|S2_trivial|S2_easy|P2) = (-?\d+)$", out, re.M)
         res = int(m[-1])
     return res, vars_
 
@@ -173,6 +173,25 @@ def main():
             rows.append(row)
             print("parts", row, flush=True)
         data["gourdon_parts"] = rows
+
+    # the Deleglise-Rivat terms (--S1, --S2-trivial, --S2-easy, --S2-hard, --P2)
+    # and its pi(x) (-d), to pin the device form of that formula term by term
+    if "dr_parts" not in data:
+        rng = random.Random(20261204)
+        xs = [10 ** e for e in range(11, 20)] + [int(10 ** rng.uniform(11, 18)) for _ in range(16)]
+        rows = []
+        for x in xs:
+            row = {"x": x}
+            for opt, key in (("--S1", "S1"), ("--S2-trivial", "S2_trivial"), ("--S2-easy", "S2_easy"),
+                             ("--S2-hard", "S2_hard"), ("--P2", "P2")):
+                r, v = run_status(x, opt)
+                row[key] = r
+                if "c" in v:
+                    row.update({"y": int(v["y"]), "z": int(v["z"]), "c": int(v["c"])})
+            row["pi"] = int(run([x, "-d"]).strip().splitlines()[-1])
+            rows.append(row)
+            print("dr", row, flush=True)
+        data["dr_parts"] = rows
 
     json.dump(data, open(OUT, "w"), indent=1)
     print("wrote", OUT)

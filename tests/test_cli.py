@@ -38,3 +38,19 @@ def test_cli_results(capsys, golden):
     assert capsys.readouterr().out.strip().splitlines()[-1] == "37607833521"
     main(["10^13"])
     assert capsys.readouterr().out.strip().splitlines()[-1] == str(golden["pi_pow10"][str(10 ** 13)])
+
+
+@pytest.mark.gpu
+def test_cli_deleglise_rivat(capsys, golden):
+    # -d and the Deleglise-Rivat term options print the reference's values
+    row = next(r for r in golden["dr_parts"] if r["x"] == 10 ** 15)
+    main(["1e15", "-d"])
+    assert capsys.readouterr().out.strip().splitlines()[-1] == str(row["pi"])
+    for opt, key in (("--S1", "S1"), ("--S2-trivial", "S2_trivial"), ("--S2-easy", "S2_easy"), ("--P2", "P2")):
+        main(["1e15", opt])
+        assert capsys.readouterr().out.strip().splitlines()[-1] == str(row[key]), opt
+
+
+def test_cli_deleglise_rivat_terms_need_large_x():
+    with pytest.raises(pcg.PrimecountError):
+        main(["1000", "--S2-easy"])

@@ -117,3 +117,24 @@ def test_pi_terms_in_sequence(pcg, golden):
     assert out.returncode == 0, out.stderr
     assert out.stdout.split() == [str(pcg.pi(x)) for x in xs]
     assert int(out.stdout.split()[0]) == golden["pi_pow10"][str(10 ** 15)]
+
+
+def test_deleglise_rivat_terms_match_reference(pcg, golden):
+    # the reference's --S1, --S2-trivial, --S2-easy, --S2-hard, --P2 and -d at
+    # 25 x from 1e11 to 1e19 (fixtures of tests/golden/gen_golden.py)
+    for row in golden["dr_parts"]:
+        x = row["x"]
+        t = pcg.pi_dr_terms(x)
+        for k in ("S1", "S2_trivial", "S2_easy", "S2_hard", "P2", "pi"):
+            assert t[k] == row[k], (x, k, t[k], row[k])
+        assert t["pi"] == t["pi_y"] + t["S1"] + t["S2_trivial"] + t["S2_easy"] + t["S2_hard"] - 1 - t["P2"]
+        assert pcg.dr_params(x)["y"] == row["y"]
+
+
+def test_deleglise_rivat_powers_of_ten(pcg, golden):
+    # README.md:163-277 of the reference: pi(10^n) by the second formula
+    for xs, v in golden["pi_pow10"].items():
+        x = int(xs)
+        if x <= 10 ** 20:
+            assert pcg.pi_deleglise_rivat(x) == v, x
+    assert pcg.pi_deleglise_rivat(1) == 0 and pcg.pi_deleglise_rivat(10 ** 6) == 78498
