@@ -1175,7 +1175,12 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
                 for (int k2 = ra + warp; k2 < rb; k2 += NT / 32) {
                   const uint32_t r = rec[k2];
                   if (r == REC_NONE) continue;
-                  const int lv = level_of(loff, li, lj, w0 + k2);
+                  // the record's level: the levels li + t whose records end at or
+                  // before it, counted by the lanes (a group has at most 64 levels)
+                  const int64_t pos = w0 + k2;
+                  int lv = li + __popc(__ballot_sync(0xffffffffu, li + lane < lj && loff[li + lane + 1] <= pos));
+                  if (lj - li > 32)
+                    lv += __popc(__ballot_sync(0xffffffffu, li + 32 + lane < lj && loff[li + 33 + lane] <= pos));
                   const uint32_t off = r & 0x3FFFFFFFu;
                   const uint64_t n = (uint64_t) low + off;
                   const uint32_t wd = off / 240, ch = wd >> 3, kw = wd & 7;
