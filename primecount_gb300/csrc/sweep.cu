@@ -1326,27 +1326,35 @@ __global__ void __launch_bounds__(NT, (NT >= 512) ? 1 : ((NT >= 256) ? 2 : 4)) k
             const uint32_t p = P.prime;
             int po = 0;
             for (int k = 0; c_small_p[k] != p; k++) po += c_small_p[k];
-            // two consecutive words per thread and round (16-byte accesses)
-            uint32_t r = (uint32_t) ((P.jlo + 2 * tid) % p);
-            const uint32_t step = (2 * NT) % p;
-            for (int w = 2 * tid; w < A.words; w += 2 * NT) {
+            // four consecutive words per thread and round (two 16-byte accesses)
+            uint32_t r = (uint32_t) ((P.jlo + 4 * tid) % p);
+            const uint32_t step = (4 * NT) % p;
+            for (int w = 4 * tid; w < A.words; w += 4 * NT) {
               uint32_t d = 0;
               if (w < wused) {
-                const ulonglong2 old = *(const ulonglong2*) (bits + w);
+                const ulonglong2 o0 = *(const ulonglong2*) (bits + w);
+                const ulonglong2 o1 = *(const ulonglong2*) (bits + w + 2);
                 const uint32_t r1 = r + 1 == p ? 0u : r + 1;
-                ulonglong2 nw;
-                nw.x = old.x & pat[po + r];
-                nw.y = (w + 1 < wused) ? (old.y & pat[po + r1]) : old.y;
-                if (nw.x != old.x || nw.y != old.y) {
-                  *(ulonglong2*) (bits + w) = nw;
-                  d = __popcll(old.x ^ nw.x) + __popcll(old.y ^ nw.y);
+                const uint32_t r2 = r1 + 1 == p ? 0u : r1 + 1;
+                const uint32_t r3 = r2 + 1 == p ? 0u : r2 + 1;
+                ulonglong2 n0, n1;
+                n0.x = o0.x & pat[po + r];
+                n0.y = (w + 1 < wused) ? (o0.y & pat[po + r1]) : o0.y;
+                n1.x = (w + 2 < wused) ? (o1.x & pat[po + r2]) : o1.x;
+                n1.y = (w + 3 < wused) ? (o1.y & pat[po + r3]) : o1.y;
+                if (n0.x != o0.x || n0.y != o0.y) {
+                  *(ulonglong2*) (bits + w) = n0;
+                  d = __popcll(o0.x ^ n0.x) + __popcll(o0.y ^ n0.y);
+                }
+                if (n1.x != o1.x || n1.y != o1.y) {
+                  *(ulonglong2*) (bits + w + 2) = n1;
+                  d += __popcll(o1.x ^ n1.x) + __popcll(o1.y ^ n1.y);
                 }
               }
               rem += d;
-              // 4 consecutive lanes own the 8 words of one chunk
-              d += __shfl_down_sync(0xffffffffu, d, 2, 4);
-              d += __shfl_down_sync(0xffffffffu, d, 1, 4);
-              if ((lane & 3) == 0 && d) ccount[w >> 3] -= d;
+              // 2 consecutive lanes own the 8 words of one chunk
+              d += __shfl_down_sync(0xffffffffu, d, 1, 2);
+              if ((lane & 1) == 0 && d) ccount[w >> 3] -= d;
               r += step;
               if (r >= p) r -= p;
             }
