@@ -22,6 +22,14 @@ static __device__ __forceinline__ uint32_t cnt8(uint32_t t)
   return (uint32_t) (v >> sh) & 15u;
 }
 
+// the low nb bits set (nb in [0, 64]; the PTX shift clamps 64 to an empty result)
+static __device__ __forceinline__ uint64_t low_bits(uint32_t nb)
+{
+  uint64_t m;
+  asm("shr.b64 %0, %1, %2;" : "=l"(m) : "l"(~0ull), "r"(64u - nb));
+  return m;
+}
+
 // bits of a 240-block for the numbers <= r (r in [0, 240))
 static __device__ __forceinline__ uint64_t mask_le(uint32_t r)
 {

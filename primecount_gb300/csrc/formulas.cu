@@ -175,9 +175,9 @@ struct PairOuter {
 };
 
 // pi(n) for n >= 6 from the PiTable {count, bits} per 240 numbers (the
-// count of a word includes 2, 3 and 5); s_mask[r] = bits of numbers <= r.
+// count of a word includes 2, 3 and 5); s_mask[r] = # wheel residues <= r.
 // Below 2^36 the word index is a 32-bit division: n / 240 = (n / 16) / 15.
-static __device__ __forceinline__ long long pi_pt(const ulonglong2* __restrict__ pt, const uint64_t* s_mask,
+static __device__ __forceinline__ long long pi_pt(const ulonglong2* __restrict__ pt, const uint8_t* s_mask,
                                                   uint64_t n)
 {
   uint64_t w;
@@ -191,17 +191,17 @@ static __device__ __forceinline__ long long pi_pt(const ulonglong2* __restrict__
     r = (uint32_t) (n - 240 * w);
   }
   const ulonglong2 e = pt[w];
-  return (long long) e.x + __popcll(e.y & s_mask[r]);
+  return (long long) e.x + __popcll(e.y & low_bits(s_mask[r]));
 }
 
 // pi(n) for n < 2^36: the word index by a 32-bit division
-static __device__ __forceinline__ long long pi_pt36(const ulonglong2* __restrict__ pt, const uint64_t* s_mask,
+static __device__ __forceinline__ long long pi_pt36(const ulonglong2* __restrict__ pt, const uint8_t* s_mask,
                                                     uint64_t n)
 {
   const uint32_t w32 = (uint32_t) (n >> 4) / 15u;
   const uint32_t r = (uint32_t) n - 240u * w32;
   const ulonglong2 e = pt[w32];
-  return (long long) e.x + __popcll(e.y & s_mask[r]);
+  return (long long) e.x + __popcll(e.y & low_bits(s_mask[r]));
 }
 
 // pi(xp / q) for the prime q = primes[i] with m = floor((2^64 - 1) / q), by
@@ -214,7 +214,7 @@ static __device__ __forceinline__ long long pi_pt36(const ulonglong2* __restrict
 // counts 2, 3 and 5 in every n) does not hold
 template <int SHAPE, bool LOWN>
 __device__ __forceinline__ long long pair_pi(const PairOuter& O, uint32_t q, uint64_t m,
-                                            const ulonglong2* __restrict__ pt, const uint64_t* s_mask)
+                                            const ulonglong2* __restrict__ pt, const uint8_t* s_mask)
 {
   uint64_t n;
   if (SHAPE == 0) {
@@ -234,7 +234,7 @@ __device__ __forceinline__ long long pair_pi(const PairOuter& O, uint32_t q, uin
 template <int SHAPE, bool LOWN>
 __device__ __forceinline__ long long pi_sum(const PairOuter& O, uint32_t lo, uint32_t hi,
                                             const uint32_t* __restrict__ primes, const uint64_t* __restrict__ magic,
-                                            const ulonglong2* __restrict__ pt, const uint64_t* s_mask)
+                                            const ulonglong2* __restrict__ pt, const uint8_t* s_mask)
 {
   long long s = 0;
   uint32_t i = lo + 1 + threadIdx.x;
@@ -258,7 +258,7 @@ __device__ __forceinline__ long long pi_sum(const PairOuter& O, uint32_t lo, uin
 template <int MODE, int SHAPE, bool LOWN>
 __device__ __forceinline__ long long pair_terms(const PairOuter& O, const uint32_t* __restrict__ primes,
                                                 const uint64_t* __restrict__ magic,
-                                                const ulonglong2* __restrict__ pt, const uint64_t* s_mask)
+                                                const ulonglong2* __restrict__ pt, const uint8_t* s_mask)
 {
   const uint32_t lo = (uint32_t) O.i_lo, hi = (uint32_t) O.i_hi;
   if (MODE == 0) {
@@ -277,7 +277,7 @@ __device__ __forceinline__ long long pair_terms(const PairOuter& O, const uint32
 template <int MODE, bool SMALL, bool LOWN>
 __device__ __forceinline__ long long outer_terms(const PairOuter& O, const uint32_t* __restrict__ primes,
                                                  const uint64_t* __restrict__ magic,
-                                                 const ulonglong2* __restrict__ pt, const uint64_t* s_mask)
+                                                 const ulonglong2* __restrict__ pt, const uint8_t* s_mask)
 {
   if (O.xp_hi != 0) return pair_terms<MODE, 2, LOWN>(O, primes, magic, pt, s_mask);
   if (SMALL) return pair_terms<MODE, 0, LOWN>(O, primes, magic, pt, s_mask);
@@ -317,8 +317,8 @@ __global__ void __launch_bounds__(256) k_pairs(const PairOuter* __restrict__ out
                                                const uint64_t* __restrict__ magic,
                                                const uint64_t* __restrict__ pibig, i128* __restrict__ partial)
 {
-  __shared__ uint64_t s_mask[240];
-  for (int r = threadIdx.x; r < 240; r += blockDim.x) s_mask[r] = mask_le((uint32_t) r);
+  __shared__ uint8_t s_mask[240];       // # wheel residues <= r
+  for (int r = threadIdx.x; r < 240; r += blockDim.x) s_mask[r] = (uint8_t) ((r / 30) * 8 + cnt8((uint32_t) (r % 30)));
   __syncthreads();
   const ulonglong2* __restrict__ pt = (const ulonglong2*) pibig;
   i128 acc = 0;

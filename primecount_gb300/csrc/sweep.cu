@@ -426,14 +426,6 @@ __device__ __forceinline__ void scan_chunks(const uint32_t* __restrict__ ccount,
   __syncthreads();
 }
 
-// the low nb bits set (nb in [0, 64]; the PTX shift clamps 64 to an empty result)
-static __device__ __forceinline__ uint64_t low_bits(uint32_t nb)
-{
-  uint64_t m;
-  asm("shr.b64 %0, %1, %2;" : "=l"(m) : "l"(~0ull), "r"(64u - nb));
-  return m;
-}
-
 // mask_le(r) from a shared table of the counts of wheel residues <= r
 static __device__ __forceinline__ uint64_t mask_le_t(const uint8_t* nbt, uint32_t r) { return low_bits(nbt[r]); }
 
