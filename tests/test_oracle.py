@@ -118,3 +118,17 @@ def test_phi_oracle(golden, ora):
     for x, a, res in golden["phi_random"]:
         if x <= 10 ** 7:
             assert ora.phi(x, a) == res, (x, a)
+
+
+def test_deleglise_rivat_fixture_consistent(golden, ora):
+    # the reference's Deleglise-Rivat terms add up to its pi(x) with pi(y) from the
+    # oracle's sieve, and its y, z, c are the oracle's parameters (x up to 1e16 here)
+    rows = [r for r in golden["dr_parts"] if r["x"] <= 10 ** 16]
+    assert len(rows) >= 8
+    for r in rows:
+        p = ora.dr_params(r["x"])
+        assert (p["y"], p["z"], p["c"]) == (r["y"], r["z"], r["c"]), r["x"]
+        pi_y = ora.pi_sieve(r["y"])
+        assert pi_y + r["S1"] + r["S2_trivial"] + r["S2_easy"] + r["S2_hard"] - 1 - r["P2"] == r["pi"], r["x"]
+        if r["x"] <= 10 ** 13:
+            assert ora.S2_hard(r["x"], r["y"], r["z"], r["c"], threads=4)[0] == r["S2_hard"], r["x"]
