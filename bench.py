@@ -57,7 +57,7 @@ UNIT = "hard-leaves/s"
 TOTAL_LEAVES_1E20 = 22178370075
 # hard leaves of D(x) at the reference's default parameters (deterministic;
 # the engine's and the oracle's counts agree)
-LEAVES = {10 ** 20: TOTAL_LEAVES_1E20}
+LEAVES = {10 ** 14: 8384338, 10 ** 16: 111012964, 10 ** 18: 1524253981, 10 ** 20: TOTAL_LEAVES_1E20}
 REF_BIN = os.path.join(ROOT, "oracle", "_ref", platform.machine(), "primecount")
 
 
